@@ -1,0 +1,66 @@
+"""Build ``libfwi_psv.so`` (the sm_103a engine + C ABI) in-tree with nvcc.
+
+Output: ``cuda_fwi_gb300/_lib/libfwi_psv.so``.  Translation units are compiled
+in parallel and only when a source is newer than its object.
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+ROOT = PKG.parent
+CSRC = PKG / "csrc"
+OUT_DIR = PKG / "_lib"
+OBJ_DIR = OUT_DIR / "obj"
+LIB = OUT_DIR / "libfwi_psv.so"
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O2,-ffp-contract=off",
+           "--expt-relaxed-constexpr", f"-I{ROOT / 'include'}", f"-I{CSRC}"]
+UNITS = ["fwi_engine.cu", "fwi_host.cpp", "fwi_refshim.cpp"]
+HEADERS = ["fwi_kernels.cuh", "fwi_host.h"]
+
+
+def nvcc() -> str:
+    return shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+
+
+def _run(cmd):
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"build failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    return r.stdout + r.stderr
+
+
+def build(force: bool = False, verbose_ptxas: bool = False) -> Path:
+    OBJ_DIR.mkdir(parents=True, exist_ok=True)
+    deps = [CSRC / h for h in HEADERS] + [ROOT / "include" / "fwi_psv.h", Path(__file__)]
+    newest_dep = max(p.stat().st_mtime for p in deps if p.exists())
+    jobs, objs = [], []
+    for u in UNITS:
+        src = CSRC / u
+        obj = OBJ_DIR / (u + ".o")
+        objs.append(obj)
+        if force or not obj.exists() or obj.stat().st_mtime < max(src.stat().st_mtime, newest_dep):
+            extra = ["-Xptxas", "-v"] if (verbose_ptxas and u.endswith(".cu")) else []
+            jobs.append([nvcc(), "-c", *ARCH, *NVFLAGS, *extra, str(src), "-o", str(obj)])
+    logs = []
+    if jobs:
+        with ThreadPoolExecutor(max_workers=len(jobs)) as ex:
+            logs = list(ex.map(_run, jobs))
+    if jobs or not LIB.exists():
+        tmp = LIB.with_suffix(".so.tmp")
+        _run([nvcc(), "-shared", *ARCH, "-o", str(tmp), *map(str, objs), "-lcudart"])
+        os.replace(tmp, LIB)
+    if verbose_ptxas:
+        print("\n".join(logs))
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv, verbose_ptxas="-v" in sys.argv))

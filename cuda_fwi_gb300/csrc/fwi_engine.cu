@@ -1,0 +1,1300 @@
+// fwi_engine.cu -- device engine behind include/fwi_psv.h.
+//
+// One engine = one padded grid (fd_grid.cu:52-71 conventions), one set of
+// materials and one acquisition (sources/receivers with their shot ids).  A
+// forward/backward call runs a *batch* of shots together: every launch covers
+// all shots of the batch (tile work-list), so the per-launch overhead is paid
+// once per time step instead of once per shot and step, and the material tile
+// is shared in L2 by the shots processed back to back.  The time loop is
+// captured into CUDA graphs and replayed.
+//
+// Reference call sequence kept (Mohammad-debug/CUDA_FWI, CUDA_week2/):
+//   forward per shot  fd_wave_model.cu:791-803   -> fwi_psv_forward
+//   residual/misfit   fd_wave_model.cu:972-1002  -> residual_kernel
+//   adjoint per shot  fd_wave_model.cu:848-859   -> fwi_psv_backward
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/fwi_psv.h"
+#include "fwi_host.h"
+#include "fwi_kernels.cuh"
+
+namespace fwi {
+
+#define CUDA_TRY(expr)                                                                   \
+    do {                                                                                 \
+        cudaError_t _e = (expr);                                                         \
+        if (_e != cudaSuccess)                                                           \
+            return fail(FWI_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(_e)); \
+    } while (0)
+
+#define FWI_TRY(expr)            \
+    do {                         \
+        int _s = (expr);         \
+        if (_s != FWI_OK) return _s; \
+    } while (0)
+
+// ---------------------------------------------------------------------------
+// small device kernels
+// ---------------------------------------------------------------------------
+
+// residual = syn - obs (in place into resid), per-row partial misfit sums in FP64
+// (fd_wave_model.cu:972-1002).  One block per receiver row.
+__global__ void residual_kernel(const float* __restrict__ syn, const float* __restrict__ obs,
+                                float* __restrict__ resid, double* __restrict__ row_misfit,
+                                int* __restrict__ blowup, int nt, double half_dt) {
+    const int r = blockIdx.x;
+    const size_t o = (size_t)r * nt;
+    double acc = 0.0;
+    int big = 0;
+    for (int t = threadIdx.x; t < nt; t += blockDim.x) {
+        const double diff = (double)syn[o + t] - (double)obs[o + t];
+        acc += half_dt * diff * diff;
+        resid[o + t] = (float)diff;
+        big |= fabs(diff) > 1.0e10;
+    }
+    __shared__ double sh[256];
+    __shared__ int sb;
+    if (threadIdx.x == 0) sb = 0;
+    sh[threadIdx.x] = acc;
+    __syncthreads();
+    if (big) atomicOr(&sb, 1);
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if ((int)threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        row_misfit[r] = sh[0];
+        if (sb) atomicOr(blowup, 1);
+    }
+}
+
+// sum the per-shot gradient triples: out[i] = sum_b in[b*n + i]
+__global__ void sum_shots_kernel(const float* __restrict__ in, float* __restrict__ out, size_t n,
+                                 int nb) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x) {
+        float s = 0.f;
+        for (int b = 0; b < nb; b++) s += in[(size_t)b * n + i];
+        out[i] = s;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// kernel dispatch on the half order
+// ---------------------------------------------------------------------------
+using LaunchFn = void (*)(dim3, dim3, cudaStream_t, const ItemDesc*, const Tile*, int, unsigned);
+
+template <int FP, bool ADJ>
+static void launch_stress(dim3 g, dim3 b, cudaStream_t s, const ItemDesc* items, const Tile* tiles,
+                          int it, unsigned flags) {
+    stress_kernel<FP, ADJ><<<g, b, 0, s>>>(items, tiles, it, flags);
+}
+template <int FP>
+static void launch_velocity(dim3 g, dim3 b, cudaStream_t s, const ItemDesc* items,
+                            const Tile* tiles, int it, unsigned flags) {
+    velocity_kernel<FP><<<g, b, 0, s>>>(items, tiles, it, flags);
+}
+
+static LaunchFn stress_fn(int fp, bool adj) {
+    switch (fp) {
+        case 1: return adj ? launch_stress<1, true> : launch_stress<1, false>;
+        case 2: return adj ? launch_stress<2, true> : launch_stress<2, false>;
+        case 3: return adj ? launch_stress<3, true> : launch_stress<3, false>;
+        case 4: return adj ? launch_stress<4, true> : launch_stress<4, false>;
+        case 5: return adj ? launch_stress<5, true> : launch_stress<5, false>;
+        case 6: return adj ? launch_stress<6, true> : launch_stress<6, false>;
+    }
+    return nullptr;
+}
+static LaunchFn velocity_fn(int fp) {
+    switch (fp) {
+        case 1: return launch_velocity<1>;
+        case 2: return launch_velocity<2>;
+        case 3: return launch_velocity<3>;
+        case 4: return launch_velocity<4>;
+        case 5: return launch_velocity<5>;
+        case 6: return launch_velocity<6>;
+    }
+    return nullptr;
+}
+
+// ---------------------------------------------------------------------------
+// device buffer
+// ---------------------------------------------------------------------------
+struct DBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    DBuf() = default;
+    DBuf(const DBuf&) = delete;
+    DBuf& operator=(const DBuf&) = delete;
+    ~DBuf() { release(); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    int ensure(size_t n) {
+        if (n <= bytes && p) return FWI_OK;
+        release();
+        if (n == 0) return FWI_OK;
+        cudaError_t e = cudaMalloc(&p, n);
+        if (e != cudaSuccess) {
+            p = nullptr;
+            cudaGetLastError();
+            return fail(FWI_ERR_NOMEM, "cudaMalloc of " + std::to_string(n) + " bytes failed: " +
+                                           cudaGetErrorString(e));
+        }
+        bytes = n;
+        return FWI_OK;
+    }
+    template <class T>
+    T* as() const {
+        return static_cast<T*>(p);
+    }
+};
+
+static size_t round_up(size_t v, size_t m) { return (v + m - 1) / m * m; }
+
+// ---------------------------------------------------------------------------
+// engine
+// ---------------------------------------------------------------------------
+struct Engine {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    // geometry / scheme
+    int nt, nzt, nxt, fpad, ppad, npml, fsurf, fdorder, tp, pitch, pnx, pnz;
+    double dt, dx, dz, hc[7];
+    std::vector<float> cpml_h;  // [6][tp]
+    // FWI window
+    int fwi_dt = 1, fwi_dx = 1, fwi_dz = 1, wx1 = 0, wx2 = 0, wz1 = 0, wz2 = 0;
+    int nft = 0, nfz = 0, nfx = 0;
+    // strategy
+    int strategy = FWI_STORE_FULL, snapshots_req = 0, grad_mode = FWI_GRAD_REFERENCE;
+    size_t budget = 0;
+    int use_graphs = 1, bx_req = 0, tz_req = 0;
+    // sizes (floats)
+    size_t field = 0, xstrip = 0, zstrip = 0, state = 0, nf = 0;
+    // device constants
+    DBuf d_mat, d_cpml, d_srcsig;
+    bool have_model = false;
+    // acquisition
+    std::vector<int> sx, sz, scomp, sshot, rx, rz, rcomp, rshot;
+    int nsrc = 0, nrec = 0;
+    // batch
+    int B = 0;
+    std::vector<int> shots;
+    std::vector<int> rows;  // receiver index of each batch row
+    std::vector<int> row_slot;
+    DBuf d_fwd, d_adj, d_ws, d_wr, d_ux, d_uz, d_grad, d_gsum, d_store, d_snap;
+    DBuf d_evcol_f, d_ev_f, d_evcol_a, d_ev_a, d_rec, d_obs, d_resid, d_rowmis, d_blow;
+    DBuf d_items_f, d_items_a, d_tiles;
+    int ntiles = 0, bx = 128, tz = 32;
+    int slots = 0;  // checkpoint slots per shot (binomial)
+    bool fwd_kept = false, have_resid = false, bwd_done = false, grad_on = true;
+    std::vector<Action> plan;
+    long long plan_cost = 0;
+    // graphs keyed by a phase name; invalidated when the batch layout changes
+    std::map<std::string, cudaGraphExec_t> graphs;
+    fwi_psv_stats stats{};
+    int64_t launches_now = 0;
+
+    ~Engine() {
+        drop_graphs();
+        if (own_stream && stream) cudaStreamDestroy(stream);
+    }
+    void drop_graphs() {
+        for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
+        graphs.clear();
+    }
+
+    int bind() { CUDA_TRY(cudaSetDevice(device)); return FWI_OK; }
+
+    // ---- setup ---------------------------------------------------------
+    int init(const fwi_psv_desc* d) {
+        nt = d->nt; nzt = d->nzt; nxt = d->nxt; fpad = d->fpad; ppad = d->ppad;
+        npml = d->npml; fsurf = d->fsurf ? 1 : 0; fdorder = d->fdorder;
+        dt = d->dt; dx = d->dx; dz = d->dz;
+        std::memcpy(hc, d->hc, sizeof hc);
+        if (fdorder < 2 || fdorder > 12 || (fdorder & 1))
+            return fail(FWI_ERR_UNSUPPORTED, "fdorder must be even and in 2..12");
+        if (fpad != fdorder / 2) return fail(FWI_ERR_INVALID, "fpad must equal fdorder/2");
+        if (npml < 0 || ppad != npml + fpad) return fail(FWI_ERR_INVALID, "ppad must equal npml + fpad");
+        if (nt < 1) return fail(FWI_ERR_INVALID, "nt must be >= 1");
+        if (nxt < 2 * ppad + 2 || nzt < (fsurf ? ppad + fpad + 2 : 2 * ppad + 2))
+            return fail(FWI_ERR_INVALID, "grid too small: need at least 2 interior cells per axis");
+        if (!(dt > 0) || !(dx > 0) || !(dz > 0)) return fail(FWI_ERR_INVALID, "dt, dx, dz must be > 0");
+        tp = 2 * (npml + 1);
+        pitch = (int)round_up(nxt, 32);
+        pnx = nxt - 2 * ppad + fpad - 1;
+        // bottom CPML offset: the reference's for fdorder 2; with a free surface at
+        // higher orders the offset keeps the layer on indices npml+1..2npml+1
+        pnz = fsurf ? nzt - 2 * ppad + fpad - 2 : nzt - 2 * ppad + fpad - 1;
+        cpml_h.assign(6 * (size_t)tp, 0.f);
+        if (npml > 0) {
+            if (!d->a || !d->b || !d->K || !d->a_half || !d->b_half || !d->K_half)
+                return fail(FWI_ERR_INVALID, "CPML profiles are required when npml > 0");
+            // Index npml is used by both the left and the right strip of the
+            // stress pass (forward_kernel_PSV_GPU.cu:847-869); it must be the
+            // identity (zero damping there), which cpml_pro yields for npower > 0.
+            if (d->a[npml] != 0.0 || d->a_half[npml] != 0.0 || d->K[npml] != 1.0 ||
+                d->K_half[npml] != 1.0)
+                return fail(FWI_ERR_UNSUPPORTED,
+                            "CPML profile index npml must be damping-free (npower > 0)");
+            for (int i = 0; i < tp; i++) {
+                cpml_h[0 * tp + i] = (float)d->a[i];
+                cpml_h[1 * tp + i] = (float)d->b[i];
+                cpml_h[2 * tp + i] = (float)(1.0 / d->K[i]);
+                cpml_h[3 * tp + i] = (float)d->a_half[i];
+                cpml_h[4 * tp + i] = (float)d->b_half[i];
+                cpml_h[5 * tp + i] = (float)(1.0 / d->K_half[i]);
+            }
+        }
+        field = (size_t)nzt * pitch;
+        xstrip = round_up((size_t)nzt * tp, 32);
+        zstrip = (size_t)tp * pitch;
+        state = round_up(5 * field + 4 * xstrip + 4 * zstrip, 64);
+        wx1 = 0; wx2 = nxt; wz1 = fsurf ? fpad : 0; wz2 = nzt;
+        update_window();
+        FWI_TRY(bind());
+        CUDA_TRY(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+        own_stream = true;
+        FWI_TRY(d_cpml.ensure(cpml_h.size() * sizeof(float) + 16));
+        CUDA_TRY(cudaMemcpy(d_cpml.p, cpml_h.data(), cpml_h.size() * sizeof(float),
+                            cudaMemcpyHostToDevice));
+        return FWI_OK;
+    }
+
+    void update_window() {
+        nft = 1 + (nt - 1) / fwi_dt;
+        nfz = 1 + (wz2 - wz1) / fwi_dz;
+        nfx = 1 + (wx2 - wx1) / fwi_dx;
+        nf = (size_t)nfz * nfx;
+    }
+
+    void invalidate_batch() {
+        drop_graphs();
+        B = 0;
+        fwd_kept = false;
+        bwd_done = false;
+    }
+
+    int set_model(const double* lam, const double* mu, const double* mu_zx, const double* rho_zp,
+                  const double* rho_xp) {
+        if (!lam || !mu || !mu_zx || !rho_zp || !rho_xp) return fail(FWI_ERR_INVALID, "null material array");
+        FWI_TRY(bind());
+        std::vector<float> h(5 * field, 0.f);
+        float* L = h.data();
+        float* M2 = L + field;
+        float* MZ = M2 + field;
+        float* BXp = MZ + field;
+        float* BZp = BXp + field;
+        for (int iz = 0; iz < nzt; iz++)
+            for (int ix = 0; ix < nxt; ix++) {
+                const size_t o = (size_t)iz * pitch + ix, c = (size_t)iz * nxt + ix;
+                L[o] = (float)(dt * lam[c]);
+                M2[o] = (float)(2.0 * dt * mu[c]);
+                if (iz < nzt - 1 && ix < nxt - 1) {
+                    const size_t a = (size_t)iz * (nxt - 1) + ix;
+                    MZ[o] = (float)(dt * mu_zx[a]);
+                    BXp[o] = (float)(dt * rho_xp[a]);
+                    BZp[o] = (float)(dt * rho_zp[a]);
+                }
+            }
+        FWI_TRY(d_mat.ensure(h.size() * sizeof(float)));
+        CUDA_TRY(cudaMemcpyAsync(d_mat.p, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice,
+                                 stream));
+        CUDA_TRY(cudaStreamSynchronize(stream));
+        have_model = true;
+        return FWI_OK;
+    }
+
+    int set_sources(int n, const int* x, const int* z, const int* comp, const int* shot,
+                    const double* sig) {
+        if (n < 0 || (n > 0 && (!x || !z || !comp || !shot || !sig)))
+            return fail(FWI_ERR_INVALID, "bad source arrays");
+        for (int i = 0; i < n; i++)
+            if (comp[i] == 2 && (x[i] < fpad || x[i] >= nxt - fpad || z[i] < fpad || z[i] >= nzt - fpad))
+                return fail(FWI_ERR_INVALID, "source " + std::to_string(i) + " outside the interior");
+        FWI_TRY(bind());
+        nsrc = n;
+        sx.assign(x, x + n); sz.assign(z, z + n); scomp.assign(comp, comp + n); sshot.assign(shot, shot + n);
+        std::vector<float> s((size_t)std::max(n, 1) * nt, 0.f);
+        for (size_t i = 0; i < (size_t)n * nt; i++) s[i] = (float)sig[i];
+        FWI_TRY(d_srcsig.ensure(s.size() * sizeof(float)));
+        CUDA_TRY(cudaMemcpy(d_srcsig.p, s.data(), s.size() * sizeof(float), cudaMemcpyHostToDevice));
+        invalidate_batch();
+        return FWI_OK;
+    }
+
+    int set_receivers(int n, const int* x, const int* z, const int* comp, const int* shot) {
+        if (n < 0 || (n > 0 && (!x || !z || !comp || !shot)))
+            return fail(FWI_ERR_INVALID, "bad receiver arrays");
+        for (int i = 0; i < n; i++)
+            if (comp[i] == 2 && (x[i] < fpad || x[i] >= nxt - fpad || z[i] < fpad || z[i] >= nzt - fpad))
+                return fail(FWI_ERR_INVALID, "receiver " + std::to_string(i) + " outside the interior");
+        nrec = n;
+        rx.assign(x, x + n); rz.assign(z, z + n); rcomp.assign(comp, comp + n); rshot.assign(shot, shot + n);
+        invalidate_batch();
+        return FWI_OK;
+    }
+
+    int set_fwi(int fdt, int fdx, int fdz, int x1, int x2, int z1, int z2) {
+        if (fdt < 1 || fdx < 1 || fdz < 1) return fail(FWI_ERR_INVALID, "FWI intervals must be >= 1");
+        if (x1 < 0 || z1 < 0 || x2 > nxt || z2 > nzt || x2 <= x1 || z2 <= z1)
+            return fail(FWI_ERR_INVALID, "FWI window outside the padded grid");
+        // Above a free surface the reference correlates mirrored stresses; the
+        // engine's gradient covers the rows from the surface down only.
+        if (fsurf && z1 < fpad)
+            return fail(FWI_ERR_UNSUPPORTED, "with a free surface the FWI window must start at row fpad or below");
+        fwi_dt = fdt; fwi_dx = fdx; fwi_dz = fdz; wx1 = x1; wx2 = x2; wz1 = z1; wz2 = z2;
+        update_window();
+        invalidate_batch();
+        return FWI_OK;
+    }
+
+    // ---- tiles -----------------------------------------------------------
+    void plan_tiles(int nb, std::vector<Tile>& t) {
+        const int nz_int = nzt - 2 * fpad;
+        bx = bx_req > 0 ? bx_req : (nxt >= 512 ? 128 : 64);
+        const int ntx = (nxt + bx - 1) / bx;
+        if (tz_req > 0) {
+            tz = tz_req;
+        } else {
+            // enough blocks for >= 8 resident blocks per SM on 152 SMs, rows >= 4
+            const long long want = 8LL * 152;
+            long long per_shot = std::max<long long>(1, want / std::max(1, nb));
+            long long ntz = std::max<long long>(1, per_shot / ntx);
+            tz = (int)std::max<long long>(4, std::min<long long>(64, (nz_int + ntz - 1) / ntz));
+        }
+        t.clear();
+        for (int x0 = 0; x0 < nxt; x0 += bx)
+            for (int z0 = fpad; z0 < nzt - fpad; z0 += tz)
+                for (int b = 0; b < nb; b++) t.push_back({b, x0, z0, std::min(z0 + tz, nzt - fpad)});
+    }
+
+    // ---- batch setup --------------------------------------------------------
+    size_t batch_bytes(int nb, int nslots, int strat) const {
+        size_t f = 4;
+        size_t b = 0;
+        b += 2 * (size_t)nb * state * f;        // fwd + adj state
+        b += 4 * (size_t)nb * field * f;        // ws, wr, ux, uz
+        b += 3 * (size_t)nb * nf * f * 2;       // grads (+ sum)
+        if (strat == FWI_STORE_FULL) b += (size_t)nb * nft * 5 * nf * f;
+        if (strat == FWI_STORE_BINOMIAL) b += (size_t)nslots * nb * state * f;
+        return b;
+    }
+
+    int setup_batch(int nb, const int* ids, bool keep) {
+        if (!have_model) return fail(FWI_ERR_STATE, "set a model first");
+        if (nb < 1 || !ids) return fail(FWI_ERR_INVALID, "empty shot batch");
+        std::vector<int> s(ids, ids + nb);
+        const bool same = (nb == B && s == shots);
+        // checkpoint slots
+        int want_slots = 0;
+        if (keep && strategy == FWI_STORE_BINOMIAL) {
+            size_t bud = budget;
+            if (bud == 0) {
+                size_t fr = 0, tot = 0;
+                CUDA_TRY(cudaMemGetInfo(&fr, &tot));
+                bud = (size_t)(0.9 * (double)(fr + allocated_bytes()));
+            }
+            const size_t base = batch_bytes(nb, 0, FWI_STORE_BINOMIAL) + fixed_bytes();
+            const size_t per_slot = (size_t)nb * state * 4;
+            long long fit = bud > base ? (long long)((bud - base) / per_slot) : 0;
+            if (snapshots_req > 0) {
+                if (fit < snapshots_req)
+                    return fail(FWI_ERR_NOMEM, "budget too small for " + std::to_string(snapshots_req) +
+                                                   " checkpoints per shot");
+                want_slots = snapshots_req;
+            } else {
+                want_slots = (int)std::min<long long>(fit, nft - 1);
+            }
+            want_slots = std::max(0, std::min(want_slots, nft - 1));
+        }
+        if (same && want_slots == slots && !tiles_dirty) return FWI_OK;
+        drop_graphs();
+        fwd_kept = false;
+        bwd_done = false;
+        if (budget > 0 && batch_bytes(nb, want_slots, keep ? strategy : -1) + fixed_bytes() > budget)
+            return fail(FWI_ERR_NOMEM, "batch does not fit the memory budget");
+        B = nb;
+        shots = s;
+        slots = want_slots;
+        // buffers
+        FWI_TRY(d_fwd.ensure((size_t)B * state * 4));
+        FWI_TRY(d_adj.ensure((size_t)B * state * 4));
+        FWI_TRY(d_ws.ensure((size_t)B * field * 4));
+        FWI_TRY(d_wr.ensure((size_t)B * field * 4));
+        FWI_TRY(d_ux.ensure((size_t)B * field * 4));
+        FWI_TRY(d_uz.ensure((size_t)B * field * 4));
+        FWI_TRY(d_grad.ensure((size_t)B * 3 * nf * 4));
+        FWI_TRY(d_gsum.ensure((size_t)3 * nf * 4));
+        if (keep && strategy == FWI_STORE_FULL) FWI_TRY(d_store.ensure((size_t)B * nft * 5 * nf * 4));
+        if (keep && strategy == FWI_STORE_BINOMIAL && slots > 0)
+            FWI_TRY(d_snap.ensure((size_t)slots * B * state * 4));
+        // receiver rows of this batch
+        rows.clear();
+        row_slot.clear();
+        std::vector<int> slot_of_row;
+        for (int b = 0; b < B; b++)
+            for (int r = 0; r < nrec; r++)
+                if (rshot[r] == shots[b] && rcomp[r] == 2) {
+                    rows.push_back(r);
+                    row_slot.push_back(b);
+                }
+        const size_t nrows = rows.size();
+        FWI_TRY(d_rec.ensure(std::max<size_t>(1, nrows) * nt * 4));
+        FWI_TRY(d_obs.ensure(std::max<size_t>(1, nrows) * nt * 4));
+        FWI_TRY(d_resid.ensure(std::max<size_t>(1, nrows) * nt * 4));
+        FWI_TRY(d_rowmis.ensure(std::max<size_t>(1, nrows) * 8));
+        FWI_TRY(d_blow.ensure(16));
+        // events per slot, grouped by column, sorted by (z, inject-before-record, index)
+        struct Ev { int x, z, kind, idx, code; };
+        std::vector<int> colf((size_t)B * (nxt + 1)), cola((size_t)B * (nxt + 1));
+        std::vector<int2> evf, eva;
+        for (int b = 0; b < B; b++) {
+            std::vector<Ev> ef, ea;
+            for (int i = 0; i < nsrc; i++)
+                if (sshot[i] == shots[b] && scomp[i] == 2) ef.push_back({sx[i], sz[i], 0, i, i});
+            for (size_t k = 0; k < nrows; k++)
+                if (row_slot[k] == b) {
+                    const int r = rows[k];
+                    ef.push_back({rx[r], rz[r], 1, r, ~(int)k});
+                    ea.push_back({rx[r], rz[r], 0, r, (int)k});
+                }
+            auto cmp = [](const Ev& u, const Ev& v) {
+                if (u.x != v.x) return u.x < v.x;
+                if (u.z != v.z) return u.z < v.z;
+                if (u.kind != v.kind) return u.kind < v.kind;
+                return u.idx < v.idx;
+            };
+            std::sort(ef.begin(), ef.end(), cmp);
+            std::sort(ea.begin(), ea.end(), cmp);
+            auto fill = [&](std::vector<Ev>& ev, std::vector<int>& col, std::vector<int2>& flat) {
+                const size_t base = flat.size();
+                int* c = col.data() + (size_t)b * (nxt + 1);
+                size_t k = 0;
+                for (int x = 0; x <= nxt; x++) {
+                    while (k < ev.size() && ev[k].x < x) k++;
+                    c[x] = (int)(k);  // relative; rebased below
+                }
+                for (auto& e : ev) flat.push_back(make_int2(e.z, e.code));
+                for (int x = 0; x <= nxt; x++) c[x] += (int)base;
+            };
+            fill(ef, colf, evf);
+            fill(ea, cola, eva);
+        }
+        FWI_TRY(d_evcol_f.ensure(colf.size() * 4));
+        FWI_TRY(d_evcol_a.ensure(cola.size() * 4));
+        FWI_TRY(d_ev_f.ensure(std::max<size_t>(1, evf.size()) * 8));
+        FWI_TRY(d_ev_a.ensure(std::max<size_t>(1, eva.size()) * 8));
+        CUDA_TRY(cudaMemcpyAsync(d_evcol_f.p, colf.data(), colf.size() * 4, cudaMemcpyHostToDevice, stream));
+        CUDA_TRY(cudaMemcpyAsync(d_evcol_a.p, cola.data(), cola.size() * 4, cudaMemcpyHostToDevice, stream));
+        if (!evf.empty())
+            CUDA_TRY(cudaMemcpyAsync(d_ev_f.p, evf.data(), evf.size() * 8, cudaMemcpyHostToDevice, stream));
+        if (!eva.empty())
+            CUDA_TRY(cudaMemcpyAsync(d_ev_a.p, eva.data(), eva.size() * 8, cudaMemcpyHostToDevice, stream));
+        // item descriptors
+        std::vector<ItemDesc> itf(B), ita(B);
+        for (int b = 0; b < B; b++) {
+            fill_item(itf[b], b, false);
+            fill_item(ita[b], b, true);
+        }
+        FWI_TRY(d_items_f.ensure(B * sizeof(ItemDesc)));
+        FWI_TRY(d_items_a.ensure(B * sizeof(ItemDesc)));
+        CUDA_TRY(cudaMemcpyAsync(d_items_f.p, itf.data(), B * sizeof(ItemDesc), cudaMemcpyHostToDevice, stream));
+        CUDA_TRY(cudaMemcpyAsync(d_items_a.p, ita.data(), B * sizeof(ItemDesc), cudaMemcpyHostToDevice, stream));
+        std::vector<Tile> t;
+        plan_tiles(B, t);
+        ntiles = (int)t.size();
+        FWI_TRY(d_tiles.ensure(t.size() * sizeof(Tile)));
+        CUDA_TRY(cudaMemcpyAsync(d_tiles.p, t.data(), t.size() * sizeof(Tile), cudaMemcpyHostToDevice, stream));
+        CUDA_TRY(cudaStreamSynchronize(stream));
+        tiles_dirty = false;
+        if (keep && strategy == FWI_STORE_BINOMIAL) plan = plan_binomial(nft, slots, &plan_cost);
+        return FWI_OK;
+    }
+    bool tiles_dirty = false;
+
+    size_t fixed_bytes() const { return d_mat.bytes + d_cpml.bytes + d_srcsig.bytes; }
+    size_t allocated_bytes() const {
+        return d_fwd.bytes + d_adj.bytes + d_ws.bytes + d_wr.bytes + d_ux.bytes + d_uz.bytes +
+               d_grad.bytes + d_gsum.bytes + d_store.bytes + d_snap.bytes + d_rec.bytes +
+               d_obs.bytes + d_resid.bytes;
+    }
+
+    void fill_item(ItemDesc& d, int b, bool adj) {
+        std::memset(&d, 0, sizeof d);
+        d.nzt = nzt; d.nxt = nxt; d.pitch = pitch; d.fpad = fpad;
+        d.ppad = ppad; d.npml = npml; d.tp = tp; d.pnx = pnx;
+        d.pnz = pnz; d.fsurf = fsurf; d.nt = nt; d.fwi_dt = fwi_dt;
+        d.fwi_dx = fwi_dx; d.fwi_dz = fwi_dz; d.wx1 = wx1; d.wx2 = wx2;
+        d.wz1 = wz1; d.wz2 = wz2; d.nfz = nfz; d.nfx = nfx;
+        d.dt = (float)dt;
+        d.inv_dt = (float)(1.0 / dt);
+        d.gscale = (float)(fwi_dt * dt);
+        for (int k = 0; k < kMaxHalf; k++) {
+            d.hx[k] = k < fpad ? (float)((1.0 / dx) * hc[k + 1]) : 0.f;
+            d.hz[k] = k < fpad ? (float)((1.0 / dz) * hc[k + 1]) : 0.f;
+        }
+        d.cpml = d_cpml.as<float>();
+        const float* m = d_mat.as<float>();
+        d.L = m; d.M2 = m + field; d.MZX = m + 2 * field; d.BX = m + 3 * field; d.BZ = m + 4 * field;
+        float* st = (adj ? d_adj.as<float>() : d_fwd.as<float>()) + (size_t)b * state;
+        d.vx = st + F_VX * field; d.vz = st + F_VZ * field; d.sxx = st + F_SXX * field;
+        d.szx = st + F_SZX * field; d.szz = st + F_SZZ * field;
+        float* cp = st + 5 * field;
+        d.mvx_x = cp; d.mvz_x = cp + xstrip; d.msxx_x = cp + 2 * xstrip; d.mszx_x = cp + 3 * xstrip;
+        float* zp = cp + 4 * xstrip;
+        d.mvx_z = zp; d.mvz_z = zp + zstrip; d.mszz_z = zp + 2 * zstrip; d.mszx_z = zp + 3 * zstrip;
+        d.We = (adj ? d_wr.as<float>() : d_ws.as<float>()) + (size_t)b * field;
+        d.ev_col = (adj ? d_evcol_a.as<int>() : d_evcol_f.as<int>()) + (size_t)b * (nxt + 1);
+        d.ev = adj ? d_ev_a.as<int2>() : d_ev_f.as<int2>();
+        d.inj = adj ? d_resid.as<float>() : d_srcsig.as<float>();
+        d.rec = d_rec.as<float>();
+        d.store = d_store.p ? d_store.as<float>() + (size_t)b * nft * 5 * nf : nullptr;
+        if (adj) {
+            d.ux = d_ux.as<float>() + (size_t)b * field;
+            d.uz = d_uz.as<float>() + (size_t)b * field;
+            d.glam = d_grad.as<float>() + (size_t)b * 3 * nf;
+            d.gmu = d.glam + nf;
+            d.grho = d.gmu + nf;
+            if (strategy == FWI_STORE_BINOMIAL) {
+                d.fwd_kind = 1;
+                d.fwd = d_fwd.as<float>() + (size_t)b * state;
+                d.fwd_fs = (long long)field;
+            } else {
+                d.fwd_kind = 0;
+                d.fwd = d.store;
+            }
+        }
+    }
+
+    // ---- launches ----------------------------------------------------------
+    void step(bool adj, int it, unsigned sflags, unsigned vflags) {
+        const dim3 g(ntiles), b(bx);
+        const ItemDesc* items = adj ? d_items_a.as<ItemDesc>() : d_items_f.as<ItemDesc>();
+        stress_fn(fpad, adj)(g, b, stream, items, d_tiles.as<Tile>(), it, sflags);
+        velocity_fn(fpad)(g, b, stream, items, d_tiles.as<Tile>(), it, vflags);
+        launches_now += 2;
+    }
+
+    // forward steps [t0, t1) of the working forward state
+    void forward_steps(int t0, int t1, bool record, bool store) {
+        for (int it = t0; it < t1; it++) {
+            unsigned sf = (store && it % fwi_dt == 0) ? FL_STORE : 0u;
+            unsigned vf = FL_INJECT | (record ? (FL_RECORD | FL_WE) : 0u);
+            step(false, it, sf, vf);
+        }
+    }
+    // adjoint steps t1-1 down to t0 (inclusive), gradient at sampled steps
+    void adjoint_steps(int t0, int t1) {
+        for (int it = t1 - 1; it >= t0; it--) {
+            unsigned sf = (grad_on && it % fwi_dt == 0) ? FL_GRAD : 0u;
+            step(true, it, sf, FL_INJECT | FL_WE);
+        }
+    }
+    int state_copy(float* dst, const float* src) {
+        CUDA_TRY(cudaMemcpyAsync(dst, src, (size_t)B * state * 4, cudaMemcpyDeviceToDevice, stream));
+        return FWI_OK;
+    }
+    float* snap(int slot) { return d_snap.as<float>() + (size_t)slot * B * state; }
+
+    // Run `body` directly or as a cached CUDA graph.
+    template <class F>
+    int run_phase(const std::string& key, F&& body) {
+        if (!use_graphs) {
+            FWI_TRY(body());
+            CUDA_TRY(cudaGetLastError());
+            return FWI_OK;
+        }
+        auto itg = graphs.find(key);
+        if (itg == graphs.end()) {
+            const int64_t before = launches_now;
+            CUDA_TRY(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+            int st = body();
+            cudaGraph_t g = nullptr;
+            cudaError_t ec = cudaStreamEndCapture(stream, &g);
+            if (st != FWI_OK) {
+                if (g) cudaGraphDestroy(g);
+                return st;
+            }
+            if (ec != cudaSuccess) return fail(FWI_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ec));
+            cudaGraphExec_t ex = nullptr;
+            ec = cudaGraphInstantiate(&ex, g, 0);
+            cudaGraphDestroy(g);
+            if (ec != cudaSuccess) return fail(FWI_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ec));
+            itg = graphs.emplace(key, ex).first;
+            graph_launches[key] = launches_now - before;
+            launches_now = before;
+        }
+        launches_now += graph_launches[key];
+        CUDA_TRY(cudaGraphLaunch(itg->second, stream));
+        return FWI_OK;
+    }
+    std::map<std::string, int64_t> graph_launches;
+
+    // ---- forward -------------------------------------------------------------
+    int forward(int nb, const int* ids, const double* obs, double* rec_out, double* misfit, int keep) {
+        FWI_TRY(bind());
+        FWI_TRY(setup_batch(nb, ids, keep != 0));
+        const size_t nrows = rows.size();
+        cudaEvent_t e0, e1;
+        CUDA_TRY(cudaEventCreate(&e0));
+        CUDA_TRY(cudaEventCreate(&e1));
+        launches_now = 0;
+        CUDA_TRY(cudaEventRecord(e0, stream));
+        if (obs && nrows) {
+            std::vector<float> o(nrows * nt);
+            for (size_t k = 0; k < nrows; k++)
+                for (int t = 0; t < nt; t++) o[k * nt + t] = (float)obs[(size_t)rows[k] * nt + t];
+            CUDA_TRY(cudaMemcpyAsync(d_obs.p, o.data(), o.size() * 4, cudaMemcpyHostToDevice, stream));
+            CUDA_TRY(cudaStreamSynchronize(stream));
+        }
+        const bool store = keep && strategy == FWI_STORE_FULL;
+        const bool ckpt = keep && strategy == FWI_STORE_BINOMIAL;
+        // checkpoint positions of the first sweep: the SAVE actions before the first ADJOINT
+        std::vector<std::pair<int, int>> saves;  // (state, slot)
+        if (ckpt)
+            for (auto& a : plan) {
+                if (a.kind == Action::ADJOINT) break;
+                if (a.kind == Action::SAVE) saves.push_back({a.b, a.a});
+            }
+        const std::string key = std::string("fwd") + (store ? "S" : "") + (ckpt ? "C" : "") +
+                                (obs ? "O" : "");
+        FWI_TRY(run_phase(key, [&]() -> int {
+            CUDA_TRY(cudaMemsetAsync(d_fwd.p, 0, (size_t)B * state * 4, stream));
+            CUDA_TRY(cudaMemsetAsync(d_ws.p, 0, (size_t)B * field * 4, stream));
+            int t = 0;
+            for (auto& sv : saves) {
+                const int tstate = sv.first * fwi_dt;
+                forward_steps(t, tstate, true, false);
+                t = tstate;
+                FWI_TRY(state_copy(snap(sv.second), d_fwd.as<float>()));
+            }
+            forward_steps(t, nt, true, store);
+            if (obs && nrows) {
+                CUDA_TRY(cudaMemsetAsync(d_blow.p, 0, 4, stream));
+                residual_kernel<<<(unsigned)nrows, 256, 0, stream>>>(
+                    d_rec.as<float>(), d_obs.as<float>(), d_resid.as<float>(), d_rowmis.as<double>(),
+                    d_blow.as<int>(), nt, 0.5 * dt);
+                launches_now++;
+            }
+            return FWI_OK;
+        }));
+        CUDA_TRY(cudaEventRecord(e1, stream));
+        std::vector<float> rec(nrows * nt);
+        std::vector<double> rm(nrows);
+        int blow = 0;
+        if (nrows && rec_out)
+            CUDA_TRY(cudaMemcpyAsync(rec.data(), d_rec.p, rec.size() * 4, cudaMemcpyDeviceToHost, stream));
+        if (nrows && obs) {
+            CUDA_TRY(cudaMemcpyAsync(rm.data(), d_rowmis.p, nrows * 8, cudaMemcpyDeviceToHost, stream));
+            CUDA_TRY(cudaMemcpyAsync(&blow, d_blow.p, 4, cudaMemcpyDeviceToHost, stream));
+        }
+        CUDA_TRY(cudaStreamSynchronize(stream));
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        stats.last_forward_ms = ms;
+        stats.launches = launches_now;
+        stats.forward_steps = (int64_t)nt;
+        stats.recompute_steps = 0;
+        stats.adjoint_steps = 0;
+        stats.device_bytes = (int64_t)(allocated_bytes() + fixed_bytes());
+        stats.snapshots = slots;
+        if (rec_out)
+            for (size_t k = 0; k < nrows; k++)
+                for (int t = 0; t < nt; t++) rec_out[(size_t)rows[k] * nt + t] = (double)rec[k * nt + t];
+        if (misfit) {
+            for (int b = 0; b < B; b++) misfit[b] = 0.0;
+            if (obs)
+                for (size_t k = 0; k < nrows; k++) misfit[row_slot[k]] += rm[k];
+        }
+        have_resid = obs != nullptr;
+        fwd_kept = keep != 0;
+        bwd_done = false;
+        if (blow) return fail(FWI_ERR_DIVERGED, "|syn - obs| exceeded 1e10 (the reference aborts here)");
+        return FWI_OK;
+    }
+
+    // ---- backward --------------------------------------------------------------
+    int backward(double* gl, double* gm, double* gr, int sum_shots) {
+        FWI_TRY(bind());
+        if (!fwd_kept) return fail(FWI_ERR_NOFORWARD, "backward needs a forward(keep=1)");
+        if (!have_resid) return fail(FWI_ERR_STATE, "backward needs observed data (forward obs) or a loaded residual");
+        if (bwd_done && strategy == FWI_STORE_BINOMIAL)
+            return fail(FWI_ERR_STATE, "the checkpointed forward was consumed by the previous backward");
+        cudaEvent_t e0, e1;
+        CUDA_TRY(cudaEventCreate(&e0));
+        CUDA_TRY(cudaEventCreate(&e1));
+        launches_now = 0;
+        long long recompute = 0;
+        CUDA_TRY(cudaEventRecord(e0, stream));
+        const std::string key = strategy == FWI_STORE_BINOMIAL ? "bwdC" : "bwdS";
+        FWI_TRY(run_phase(key, [&]() -> int {
+            CUDA_TRY(cudaMemsetAsync(d_adj.p, 0, (size_t)B * state * 4, stream));
+            CUDA_TRY(cudaMemsetAsync(d_wr.p, 0, (size_t)B * field * 4, stream));
+            CUDA_TRY(cudaMemsetAsync(d_ux.p, 0, (size_t)B * field * 4, stream));
+            CUDA_TRY(cudaMemsetAsync(d_uz.p, 0, (size_t)B * field * 4, stream));
+            CUDA_TRY(cudaMemsetAsync(d_grad.p, 0, (size_t)B * 3 * nf * 4, stream));
+            if (strategy != FWI_STORE_BINOMIAL) {
+                adjoint_steps(0, nt);
+                return FWI_OK;
+            }
+            // Execute the binomial plan.  The first sweep of forward() already
+            // placed the SAVEs that precede the first ADJOINT; start after them.
+            size_t k = 0;
+            int last_slot = -1, last_state = 0;
+            while (k < plan.size() && plan[k].kind != Action::ADJOINT) {
+                if (plan[k].kind == Action::SAVE) { last_slot = plan[k].a; last_state = plan[k].b; }
+                k++;
+            }
+            // working buffer: state of the last prefix checkpoint, advanced to nft-1
+            if (last_slot >= 0) FWI_TRY(state_copy(d_fwd.as<float>(), snap(last_slot)));
+            else CUDA_TRY(cudaMemsetAsync(d_fwd.p, 0, (size_t)B * state * 4, stream));
+            forward_steps(last_state * fwi_dt, (nft - 1) * fwi_dt, false, false);
+            recompute += (nft - 1) - last_state;
+            for (; k < plan.size(); k++) {
+                const Action& a = plan[k];
+                switch (a.kind) {
+                    case Action::ADVANCE:
+                        forward_steps(a.a * fwi_dt, a.b * fwi_dt, false, false);
+                        recompute += a.b - a.a;
+                        break;
+                    case Action::SAVE:
+                        FWI_TRY(state_copy(snap(a.a), d_fwd.as<float>()));
+                        break;
+                    case Action::RESTORE:
+                        if (a.a < 0) CUDA_TRY(cudaMemsetAsync(d_fwd.p, 0, (size_t)B * state * 4, stream));
+                        else FWI_TRY(state_copy(d_fwd.as<float>(), snap(a.a)));
+                        break;
+                    case Action::ADJOINT: {
+                        const int t0 = a.a * fwi_dt, t1 = std::min(nt, (a.a + 1) * fwi_dt);
+                        adjoint_steps(t0, t1);
+                        break;
+                    }
+                }
+            }
+            return FWI_OK;
+        }));
+        if (sum_shots && B > 1) {
+            sum_shots_kernel<<<592, 256, 0, stream>>>(d_grad.as<float>(), d_gsum.as<float>(), 3 * nf, B);
+            launches_now++;
+        }
+        CUDA_TRY(cudaEventRecord(e1, stream));
+        const bool summed = sum_shots && B > 1;
+        const size_t ntrip = summed ? 1 : (size_t)B;
+        std::vector<float> g(ntrip * 3 * nf);
+        CUDA_TRY(cudaMemcpyAsync(g.data(), summed ? d_gsum.p : d_grad.p, g.size() * 4,
+                                 cudaMemcpyDeviceToHost, stream));
+        CUDA_TRY(cudaStreamSynchronize(stream));
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        stats.last_backward_ms = ms;
+        stats.launches = launches_now;
+        stats.adjoint_steps = nt;
+        stats.recompute_steps = strategy == FWI_STORE_BINOMIAL
+                                    ? (recompute > 0 ? recompute : plan_cost) * fwi_dt
+                                    : 0;
+        for (size_t s = 0; s < ntrip; s++)
+            for (size_t i = 0; i < nf; i++) {
+                const float* t = g.data() + s * 3 * nf;
+                if (gl) gl[s * nf + i] = t[i];
+                if (gm) gm[s * nf + i] = t[nf + i];
+                if (gr) gr[s * nf + i] = t[2 * nf + i];
+            }
+        bwd_done = true;
+        return FWI_OK;
+    }
+
+    // Residual rows of the current batch from a [nrec][nt] host array (receiver order).
+    int load_residual(const double* sig) {
+        FWI_TRY(bind());
+        const size_t nrows = rows.size();
+        if (!nrows) { have_resid = true; return FWI_OK; }
+        std::vector<float> r(nrows * nt);
+        for (size_t k = 0; k < nrows; k++)
+            for (int t = 0; t < nt; t++) r[k * nt + t] = (float)sig[(size_t)rows[k] * nt + t];
+        CUDA_TRY(cudaMemcpyAsync(d_resid.p, r.data(), r.size() * 4, cudaMemcpyHostToDevice, stream));
+        CUDA_TRY(cudaStreamSynchronize(stream));
+        have_resid = true;
+        return FWI_OK;
+    }
+    // FWI storage of batch slot 0 to/from the reference layout (5 arrays [nft][nfz][nfx],
+    // order vx, vz, sxx, szx, szz; velocities divided by dt as the reference stores them).
+    int storage_io(double* const f[5], bool upload) {
+        FWI_TRY(bind());
+        if (!d_store.p) return fail(FWI_ERR_STATE, "no FWI storage allocated");
+        std::vector<float> h((size_t)nft * 5 * nf);
+        if (!upload) CUDA_TRY(cudaMemcpy(h.data(), d_store.p, h.size() * 4, cudaMemcpyDeviceToHost));
+        for (int tf = 0; tf < nft; tf++)
+            for (int q = 0; q < 5; q++) {
+                if (!f[q]) continue;
+                float* blk = h.data() + ((size_t)tf * 5 + q) * nf;
+                double* ref = f[q] + (size_t)tf * nf;
+                for (size_t i = 0; i < nf; i++) {
+                    if (upload) blk[i] = (float)ref[i];
+                    else ref[i] = blk[i];
+                }
+            }
+        if (upload) CUDA_TRY(cudaMemcpy(d_store.p, h.data(), h.size() * 4, cudaMemcpyHostToDevice));
+        return FWI_OK;
+    }
+    // CPML memory of batch slot 0 in the reference layouts, order
+    // mem_vx_x, mem_vx_z, mem_vz_x, mem_vz_z, mem_sxx_x, mem_szx_x, mem_szz_z, mem_szx_z.
+    int read_cpml(int which, double* const m[8]) {
+        FWI_TRY(bind());
+        const float* st = (which ? d_adj.as<float>() : d_fwd.as<float>()) + 5 * field;
+        std::vector<float> h(4 * xstrip + 4 * zstrip);
+        CUDA_TRY(cudaMemcpy(h.data(), st, h.size() * 4, cudaMemcpyDeviceToHost));
+        // device order: x-strips vx_x, vz_x, sxx_x, szx_x; z-strips vx_z, vz_z, szz_z, szx_z
+        const int xs_of[8] = {0, -1, 1, -1, 2, 3, -1, -1};
+        const int zs_of[8] = {-1, 0, -1, 1, -1, -1, 2, 3};
+        for (int q = 0; q < 8; q++) {
+            if (!m[q]) continue;
+            if (xs_of[q] >= 0) {
+                const float* src = h.data() + xs_of[q] * xstrip;
+                for (size_t i = 0; i < (size_t)nzt * tp; i++) m[q][i] = src[i];
+            } else {
+                const float* src = h.data() + 4 * xstrip + zs_of[q] * zstrip;
+                for (int p = 0; p < tp; p++)
+                    for (int ix = 0; ix < nxt; ix++) m[q][(size_t)p * nxt + ix] = src[(size_t)p * pitch + ix];
+            }
+        }
+        return FWI_OK;
+    }
+
+    int energy(int slot, double* Ws, double* Wr) {
+        FWI_TRY(bind());
+        if (slot < 0 || slot >= B) return fail(FWI_ERR_INVALID, "bad batch slot");
+        std::vector<float> h(field);
+        auto get = [&](const DBuf& src, double* out) -> int {
+            if (!out) return FWI_OK;
+            CUDA_TRY(cudaMemcpy(h.data(), src.as<float>() + (size_t)slot * field, field * 4,
+                                cudaMemcpyDeviceToHost));
+            for (int iz = 0; iz < nzt; iz++)
+                for (int ix = 0; ix < nxt; ix++) out[(size_t)iz * nxt + ix] = h[(size_t)iz * pitch + ix];
+            return FWI_OK;
+        };
+        FWI_TRY(get(d_ws, Ws));
+        FWI_TRY(get(d_wr, Wr));
+        return FWI_OK;
+    }
+
+    int wavefield(int which, int slot, double* out[5]) {
+        FWI_TRY(bind());
+        if (slot < 0 || slot >= B) return fail(FWI_ERR_INVALID, "bad batch slot");
+        const float* st = (which ? d_adj.as<float>() : d_fwd.as<float>()) + (size_t)slot * state;
+        std::vector<float> h(5 * field);
+        CUDA_TRY(cudaMemcpy(h.data(), st, h.size() * 4, cudaMemcpyDeviceToHost));
+        for (int f = 0; f < 5; f++) {
+            if (!out[f]) continue;
+            for (int iz = 0; iz < nzt; iz++)
+                for (int ix = 0; ix < nxt; ix++)
+                    out[f][(size_t)iz * nxt + ix] = h[f * field + (size_t)iz * pitch + ix];
+        }
+        return FWI_OK;
+    }
+};
+
+}  // namespace fwi
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+using fwi::Engine;
+using fwi::fail;
+
+struct fwi_psv_engine {
+    Engine e;
+};
+
+#define GUARD_ENGINE(h) \
+    if (!(h)) return fail(FWI_ERR_INVALID, "null engine")
+
+extern "C" {
+
+int fwi_psv_abi_version(void) { return FWI_PSV_ABI_VERSION; }
+
+const char* fwi_psv_strerror(int s) {
+    switch (s) {
+        case FWI_OK: return "ok";
+        case FWI_ERR_INVALID: return "invalid argument";
+        case FWI_ERR_UNSUPPORTED: return "unsupported configuration";
+        case FWI_ERR_NOMEM: return "out of memory";
+        case FWI_ERR_CUDA: return "CUDA error";
+        case FWI_ERR_STATE: return "call out of order";
+        case FWI_ERR_DIVERGED: return "wavefield diverged";
+        case FWI_ERR_NOFORWARD: return "no retained forward pass";
+        case FWI_ERR_NODEVICE: return "no CUDA device";
+    }
+    return "unknown status";
+}
+
+const char* fwi_psv_last_error(void) { return fwi::last_error(); }
+
+int fwi_psv_holberg(int fdorder, int max_rel_err, double hc[7]) {
+    if (!hc) return fail(FWI_ERR_INVALID, "null hc");
+    return fwi::holberg(fdorder, max_rel_err, hc);
+}
+
+int fwi_psv_cpml_profile(int npml, double dh, double fpml, double npower, double k_max_pml,
+                         double rcoef, double damp_v_pml, double dt, double* a, double* b,
+                         double* K, double* a_half, double* b_half, double* K_half) {
+    if (npml < 1 || !a || !b || !K || !a_half || !b_half || !K_half)
+        return fail(FWI_ERR_INVALID, "npml must be >= 1 and all profile arrays given");
+    if (!(dh > 0) || !(rcoef > 0)) return fail(FWI_ERR_INVALID, "dh and rcoef must be > 0");
+    fwi::cpml_profile(npml, dh, fpml, npower, k_max_pml, rcoef, damp_v_pml, dt, a, b, K, a_half,
+                      b_half, K_half);
+    return FWI_OK;
+}
+
+int fwi_psv_total_grid(int nx, int nz, int fdorder, int npml, int fsurf, int* fpad, int* ppad,
+                       int* nxt, int* nzt) {
+    if (!fpad || !ppad || !nxt || !nzt || nx < 1 || nz < 1 || npml < 0)
+        return fail(FWI_ERR_INVALID, "bad grid arguments");
+    if (fdorder < 2 || fdorder > 12 || (fdorder & 1)) return fail(FWI_ERR_INVALID, "bad fdorder");
+    fwi::total_grid(nx, nz, fdorder, npml, fsurf, fpad, ppad, nxt, nzt);
+    return FWI_OK;
+}
+
+int fwi_psv_wavelet(double* signal, int nt, double dt, double amp, double fc, double ts, int shape) {
+    if (!signal || nt < 0 || !(fc > 0)) return fail(FWI_ERR_INVALID, "bad wavelet arguments");
+    if (shape != 1) return fail(FWI_ERR_UNSUPPORTED, "only shape 1 (Ricker) exists");
+    fwi::wavelet(signal, nt, dt, amp, fc, ts, shape);
+    return FWI_OK;
+}
+
+int fwi_psv_average_parameters(int nzt, int nxt, const double* mu, const double* rho,
+                               double* mu_zx, double* rho_zp, double* rho_xp) {
+    if (nzt < 2 || nxt < 2 || !mu || !rho || !mu_zx || !rho_zp || !rho_xp)
+        return fail(FWI_ERR_INVALID, "bad averaging arguments");
+    fwi::average_parameters(nzt, nxt, mu, rho, mu_zx, rho_zp, rho_xp);
+    return FWI_OK;
+}
+
+int fwi_psv_checkpoint_plan(int nsteps, int slots, int* actions, int cap, int* count,
+                            long long* forward_steps) {
+    if (nsteps < 0 || slots < 0 || !count) return fail(FWI_ERR_INVALID, "bad plan arguments");
+    long long cost = 0;
+    const std::vector<fwi::Action> plan = fwi::plan_binomial(nsteps, slots, &cost);
+    *count = (int)plan.size();
+    if (forward_steps) *forward_steps = cost;
+    if (!actions || cap < (int)plan.size()) return fail(FWI_ERR_INVALID, "action buffer too small");
+    for (size_t i = 0; i < plan.size(); i++) {
+        actions[3 * i] = plan[i].kind;
+        actions[3 * i + 1] = plan[i].a;
+        actions[3 * i + 2] = plan[i].b;
+    }
+    return FWI_OK;
+}
+
+int fwi_psv_create(const fwi_psv_desc* desc, int device, fwi_psv_engine** out) {
+    if (!desc || !out) return fail(FWI_ERR_INVALID, "null argument");
+    *out = nullptr;
+    int n = 0;
+    cudaError_t ce = cudaGetDeviceCount(&n);
+    if (ce != cudaSuccess || n == 0) {
+        cudaGetLastError();
+        return fail(FWI_ERR_NODEVICE, std::string("no CUDA device: ") + cudaGetErrorString(ce));
+    }
+    if (device < 0 || device >= n) return fail(FWI_ERR_INVALID, "bad device index");
+    std::unique_ptr<fwi_psv_engine> h(new (std::nothrow) fwi_psv_engine());
+    if (!h) return fail(FWI_ERR_NOMEM, "host allocation failed");
+    h->e.device = device;
+    int s = h->e.init(desc);
+    if (s != FWI_OK) return s;
+    *out = h.release();
+    return FWI_OK;
+}
+
+int fwi_psv_destroy(fwi_psv_engine* e) {
+    if (!e) return FWI_OK;
+    cudaSetDevice(e->e.device);
+    if (e->e.stream) cudaStreamSynchronize(e->e.stream);
+    delete e;
+    return FWI_OK;
+}
+
+int fwi_psv_set_stream(fwi_psv_engine* h, void* s) {
+    GUARD_ENGINE(h);
+    Engine& e = h->e;
+    if (e.own_stream && e.stream) {
+        cudaStreamSynchronize(e.stream);
+        cudaStreamDestroy(e.stream);
+    }
+    e.drop_graphs();
+    if (s) {
+        e.stream = static_cast<cudaStream_t>(s);
+        e.own_stream = false;
+    } else {
+        cudaSetDevice(e.device);
+        if (cudaStreamCreateWithFlags(&e.stream, cudaStreamNonBlocking) != cudaSuccess)
+            return fail(FWI_ERR_CUDA, "stream creation failed");
+        e.own_stream = true;
+    }
+    return FWI_OK;
+}
+
+int fwi_psv_set_model(fwi_psv_engine* h, const double* lam, const double* mu, const double* mu_zx,
+                      const double* rho_zp, const double* rho_xp) {
+    GUARD_ENGINE(h);
+    return h->e.set_model(lam, mu, mu_zx, rho_zp, rho_xp);
+}
+
+int fwi_psv_set_model_lmr(fwi_psv_engine* h, const double* lam, const double* mu, const double* rho) {
+    GUARD_ENGINE(h);
+    if (!lam || !mu || !rho) return fail(FWI_ERR_INVALID, "null material array");
+    Engine& e = h->e;
+    const size_t na = (size_t)(e.nzt - 1) * (e.nxt - 1);
+    std::vector<double> mz(na), rz(na), rx(na);
+    fwi::average_parameters(e.nzt, e.nxt, mu, rho, mz.data(), rz.data(), rx.data());
+    return e.set_model(lam, mu, mz.data(), rz.data(), rx.data());
+}
+
+int fwi_psv_set_sources(fwi_psv_engine* h, int n, const int* x, const int* z, const int* comp,
+                        const int* shot, const double* signal) {
+    GUARD_ENGINE(h);
+    return h->e.set_sources(n, x, z, comp, shot, signal);
+}
+
+int fwi_psv_set_receivers(fwi_psv_engine* h, int n, const int* x, const int* z, const int* comp,
+                          const int* shot) {
+    GUARD_ENGINE(h);
+    return h->e.set_receivers(n, x, z, comp, shot);
+}
+
+int fwi_psv_set_fwi(fwi_psv_engine* h, int fdt, int fdx, int fdz, int x1, int x2, int z1, int z2) {
+    GUARD_ENGINE(h);
+    return h->e.set_fwi(fdt, fdx, fdz, x1, x2, z1, z2);
+}
+
+int fwi_psv_set_strategy(fwi_psv_engine* h, int strategy, int snapshots, size_t budget) {
+    GUARD_ENGINE(h);
+    if (strategy != FWI_STORE_FULL && strategy != FWI_STORE_BINOMIAL && strategy != FWI_STORE_RANDOM)
+        return fail(FWI_ERR_INVALID, "unknown strategy");
+    if (strategy == FWI_STORE_RANDOM)
+        return fail(FWI_ERR_UNSUPPORTED, "random-boundary reconstruction is not available in this build");
+    if (snapshots < 0) return fail(FWI_ERR_INVALID, "snapshots must be >= 0");
+    Engine& e = h->e;
+    e.strategy = strategy;
+    e.snapshots_req = snapshots;
+    e.budget = budget;
+    e.invalidate_batch();
+    return FWI_OK;
+}
+
+int fwi_psv_set_gradient_mode(fwi_psv_engine* h, int mode) {
+    GUARD_ENGINE(h);
+    if (mode != FWI_GRAD_REFERENCE && mode != FWI_GRAD_EXACT) return fail(FWI_ERR_INVALID, "unknown mode");
+    if (mode == FWI_GRAD_EXACT) return fail(FWI_ERR_UNSUPPORTED, "exact discrete adjoint not available in this build");
+    h->e.grad_mode = mode;
+    return FWI_OK;
+}
+
+int fwi_psv_set_exec(fwi_psv_engine* h, int use_graphs, int block_x, int tile_z) {
+    GUARD_ENGINE(h);
+    if (block_x < 0 || block_x > 256 || (block_x % 32) != 0 || tile_z < 0)
+        return fail(FWI_ERR_INVALID, "block_x must be a multiple of 32 in 32..256, tile_z >= 0");
+    Engine& e = h->e;
+    e.use_graphs = use_graphs ? 1 : 0;
+    e.bx_req = block_x;
+    e.tz_req = tile_z;
+    e.tiles_dirty = true;
+    e.drop_graphs();
+    return FWI_OK;
+}
+
+int fwi_psv_forward(fwi_psv_engine* h, int nshots, const int* shots, const double* obs,
+                    double* rec_out, double* misfit, int keep) {
+    GUARD_ENGINE(h);
+    return h->e.forward(nshots, shots, obs, rec_out, misfit, keep);
+}
+
+int fwi_psv_backward(fwi_psv_engine* h, double* gl, double* gm, double* gr, int sum_shots) {
+    GUARD_ENGINE(h);
+    return h->e.backward(gl, gm, gr, sum_shots);
+}
+
+int fwi_psv_energy(fwi_psv_engine* h, int slot, double* Ws, double* Wr) {
+    GUARD_ENGINE(h);
+    return h->e.energy(slot, Ws, Wr);
+}
+
+int fwi_psv_wavefield(fwi_psv_engine* h, int which, int slot, double* vx, double* vz, double* sxx,
+                      double* szx, double* szz) {
+    GUARD_ENGINE(h);
+    double* out[5] = {vx, vz, sxx, szx, szz};
+    return h->e.wavefield(which, slot, out);
+}
+
+int fwi_psv_get_stats(fwi_psv_engine* h, fwi_psv_stats* out) {
+    GUARD_ENGINE(h);
+    if (!out) return fail(FWI_ERR_INVALID, "null stats");
+    *out = h->e.stats;
+    return FWI_OK;
+}
+
+// ---- reference-shaped calls ------------------------------------------------
+// One engine per host thread is cached and reused while the grid, scheme and
+// CPML profiles stay the same (the reference calls these once per shot).
+namespace {
+struct RefCache {
+    std::unique_ptr<fwi_psv_engine> h;
+    fwi_psv_desc d{};
+    std::vector<double> prof;
+};
+thread_local RefCache g_ref;
+
+int ref_engine(const fwi_psv_desc& d, Engine** out) {
+    const int tp = 2 * (d.npml + 1);
+    std::vector<double> prof;
+    if (d.npml > 0)
+        for (const double* p : {d.a, d.b, d.K, d.a_half, d.b_half, d.K_half}) {
+            if (!p) return fail(FWI_ERR_INVALID, "CPML profiles are required when npml > 0");
+            prof.insert(prof.end(), p, p + tp);
+        }
+    const bool same = g_ref.h && g_ref.d.nt == d.nt && g_ref.d.nzt == d.nzt && g_ref.d.nxt == d.nxt &&
+                      g_ref.d.fpad == d.fpad && g_ref.d.ppad == d.ppad && g_ref.d.npml == d.npml &&
+                      g_ref.d.fsurf == d.fsurf && g_ref.d.fdorder == d.fdorder &&
+                      g_ref.d.dt == d.dt && g_ref.d.dx == d.dx && g_ref.d.dz == d.dz &&
+                      std::memcmp(g_ref.d.hc, d.hc, sizeof d.hc) == 0 && g_ref.prof == prof;
+    if (!same) {
+        if (g_ref.h) fwi_psv_destroy(g_ref.h.release());
+        fwi_psv_engine* h = nullptr;
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess) dev = 0;
+        FWI_TRY(fwi_psv_create(&d, dev, &h));
+        g_ref.h.reset(h);
+        g_ref.d = d;
+        g_ref.prof = prof;
+        // per-shot calls with changing models: plain launches, no graph capture
+        h->e.use_graphs = 0;
+    }
+    *out = &g_ref.h->e;
+    return FWI_OK;
+}
+
+fwi_psv_desc make_desc(int nt, int nzt, int nxt, int fpad, int ppad, double dt, double dx,
+                       double dz, int fsurf, const double* hc, int fdorder, int npml,
+                       const double* a, const double* b, const double* K, const double* ah,
+                       const double* bh, const double* Kh) {
+    fwi_psv_desc d{};
+    d.nt = nt; d.nzt = nzt; d.nxt = nxt; d.fpad = fpad; d.ppad = ppad; d.npml = npml;
+    d.fsurf = fsurf; d.fdorder = fdorder; d.dt = dt; d.dx = dx; d.dz = dz;
+    for (int i = 0; i < 7; i++) d.hc[i] = hc ? hc[i] : 0.0;
+    d.a = a; d.b = b; d.K = K; d.a_half = ah; d.b_half = bh; d.K_half = Kh;
+    return d;
+}
+}  // namespace
+
+int fwi_psv_forward_kernel(int ishot, int nt, int nzt, int nxt, int fpad, int ppad, double dt,
+                           double dx, double dz, int snap_interval, int fsurf, const double* hc,
+                           int fdorder, double* vx, double* vz, double* sxx, double* szx,
+                           double* szz, double* We, const double* lam, const double* mu,
+                           const double* mu_zx, const double* rho_zp, const double* rho_xp,
+                           int npml, const double* a, const double* b, const double* K,
+                           const double* a_half, const double* b_half, const double* K_half,
+                           double* mem_vx_x, double* mem_vx_z, double* mem_vz_x,
+                           double* mem_vz_z, double* mem_sxx_x, double* mem_szx_x,
+                           double* mem_szz_z, double* mem_szx_z, int nsrc, const int* src_x,
+                           const int* src_z, const int* src_comp, const double* src_signal,
+                           const int* source_to_fire_shot, int nrec, const int* rec_x,
+                           const int* rec_z, const int* rec_comp, double* rec_signal,
+                           const int* receiver_to_record_shot, int fwinv, int fwi_dt,
+                           int fwi_dx, int fwi_dz, int fwi_x1, int fwi_x2, int fwi_z1,
+                           int fwi_z2, double* fwi_vx, double* fwi_vz, double* fwi_sxx,
+                           double* fwi_szx, double* fwi_szz) {
+    (void)snap_interval;  // the CSV snapshot writer is not part of the engine
+    if (!hc) return fail(FWI_ERR_INVALID, "null hc");
+    fwi_psv_desc d = make_desc(nt, nzt, nxt, fpad, ppad, dt, dx, dz, fsurf, hc, fdorder, npml, a,
+                               b, K, a_half, b_half, K_half);
+    Engine* e = nullptr;
+    FWI_TRY(ref_engine(d, &e));
+    FWI_TRY(e->set_model(lam, mu, mu_zx, rho_zp, rho_xp));
+    FWI_TRY(e->set_sources(nsrc, src_x, src_z, src_comp, source_to_fire_shot, src_signal));
+    FWI_TRY(e->set_receivers(nrec, rec_x, rec_z, rec_comp, receiver_to_record_shot));
+    if (fwinv) FWI_TRY(e->set_fwi(fwi_dt, fwi_dx, fwi_dz, fwi_x1, fwi_x2, fwi_z1, fwi_z2));
+    else FWI_TRY(e->set_fwi(1, 1, 1, 0, nxt, 0, nzt));
+    e->strategy = FWI_STORE_FULL;
+    FWI_TRY(e->forward(1, &ishot, nullptr, rec_signal, nullptr, fwinv ? 1 : 0));
+    double* w[5] = {vx, vz, sxx, szx, szz};
+    FWI_TRY(e->wavefield(0, 0, w));
+    if (We) FWI_TRY(e->energy(0, We, nullptr));
+    double* m[8] = {mem_vx_x, mem_vx_z, mem_vz_x, mem_vz_z, mem_sxx_x, mem_szx_x, mem_szz_z, mem_szx_z};
+    FWI_TRY(e->read_cpml(0, m));
+    if (fwinv) {
+        double* f[5] = {fwi_vx, fwi_vz, fwi_sxx, fwi_szx, fwi_szz};
+        FWI_TRY(e->storage_io(f, false));
+    }
+    return FWI_OK;
+}
+
+int fwi_psv_adjoint_kernel(int ishot, int nt, int nzt, int nxt, int fpad, int ppad, double dt,
+                           double dx, double dz, int snap_interval, int fsurf, const double* hc,
+                           int fdorder, double* vx, double* vz, double* sxx, double* szx,
+                           double* szz, double* We, const double* lam, const double* mu,
+                           const double* mu_zx, const double* rho_zp, const double* rho_xp,
+                           int npml, const double* a, const double* b, const double* K,
+                           const double* a_half, const double* b_half, const double* K_half,
+                           double* mem_vx_x, double* mem_vx_z, double* mem_vz_x,
+                           double* mem_vz_z, double* mem_sxx_x, double* mem_szx_x,
+                           double* mem_szz_z, double* mem_szx_z, int nsrc, const int* src_x,
+                           const int* src_z, const int* src_comp, const double* src_signal,
+                           const int* source_to_fire_shot, int fwinv, int fwi_dt, int fwi_dx,
+                           int fwi_dz, int fwi_x1, int fwi_x2, int fwi_z1, int fwi_z2,
+                           const double* fwi_vx, const double* fwi_vz, const double* fwi_sxx,
+                           const double* fwi_szx, const double* fwi_szz, double* grad_lam,
+                           double* grad_mu, double* grad_rho) {
+    (void)snap_interval;
+    if (!hc) return fail(FWI_ERR_INVALID, "null hc");
+    fwi_psv_desc d = make_desc(nt, nzt, nxt, fpad, ppad, dt, dx, dz, fsurf, hc, fdorder, npml, a,
+                               b, K, a_half, b_half, K_half);
+    Engine* e = nullptr;
+    FWI_TRY(ref_engine(d, &e));
+    FWI_TRY(e->set_model(lam, mu, mu_zx, rho_zp, rho_xp));
+    // The adjoint's sources are the receivers carrying the residual
+    // (fd_wave_model.cu:848-859 passes receiver.* as the source arguments).
+    FWI_TRY(e->set_sources(0, nullptr, nullptr, nullptr, nullptr, nullptr));
+    FWI_TRY(e->set_receivers(nsrc, src_x, src_z, src_comp, source_to_fire_shot));
+    FWI_TRY(e->set_fwi(fwi_dt, fwi_dx, fwi_dz, fwi_x1, fwi_x2, fwi_z1, fwi_z2));
+    e->strategy = FWI_STORE_FULL;
+    FWI_TRY(e->setup_batch(1, &ishot, true));
+    if (fwinv) {
+        if (!fwi_vx || !fwi_vz || !fwi_sxx || !fwi_szx || !fwi_szz)
+            return fail(FWI_ERR_INVALID, "FWI storage arrays required when fwinv");
+        double* f[5] = {const_cast<double*>(fwi_vx), const_cast<double*>(fwi_vz),
+                        const_cast<double*>(fwi_sxx), const_cast<double*>(fwi_szx),
+                        const_cast<double*>(fwi_szz)};
+        FWI_TRY(e->storage_io(f, true));
+    }
+    FWI_TRY(e->load_residual(src_signal));
+    e->fwd_kept = true;
+    e->bwd_done = false;
+    e->grad_on = fwinv != 0;
+    int st = e->backward(grad_lam, grad_mu, grad_rho, 0);
+    e->grad_on = true;
+    FWI_TRY(st);
+    double* w[5] = {vx, vz, sxx, szx, szz};
+    FWI_TRY(e->wavefield(1, 0, w));
+    if (We) FWI_TRY(e->energy(0, nullptr, We));
+    double* m[8] = {mem_vx_x, mem_vx_z, mem_vz_x, mem_vz_z, mem_sxx_x, mem_szx_x, mem_szz_z, mem_szx_z};
+    FWI_TRY(e->read_cpml(1, m));
+    return FWI_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,147 @@
+"""Pythonic wrapper of the engine C ABI (``include/fwi_psv.h``).
+
+Mirrors the reference's per-shot propagator pair (Mohammad-debug/CUDA_FWI,
+CUDA_week2/fd_kernel.cuh:75-173) as a batched forward/backward pair:
+
+    eng = Engine(problem)                 # grid, scheme, CPML, materials, acquisition
+    rec, misfit = eng.forward(shots, obs, keep=True)
+    g_lam, g_mu, g_rho = eng.backward(sum_shots=True)
+
+All work runs on the GPU; there is no CPU path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _capi
+from ._capi import check, pd, pi
+from .problem import Problem
+
+STRATEGIES = {"full": _capi.FWI_STORE_FULL, "binomial": _capi.FWI_STORE_BINOMIAL,
+              "random": _capi.FWI_STORE_RANDOM}
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _i32(a):
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+class Engine:
+    def __init__(self, problem: Problem, device: int = 0, set_model: bool = True):
+        self.p = problem
+        L = _capi.lib()
+        self._cp = {k: _f64(v) for k, v in problem.cpml.items()}
+        d = _capi.Desc()
+        for k in ("nt", "nzt", "nxt", "fpad", "ppad", "npml", "fsurf", "fdorder"):
+            setattr(d, k, int(getattr(problem, k)))
+        d.dt, d.dx, d.dz = problem.dt, problem.dx, problem.dz
+        for i in range(7):
+            d.hc[i] = float(problem.hc[i])
+        for k in ("a", "b", "K", "a_half", "b_half", "K_half"):
+            setattr(d, k, pd(self._cp[k]))
+        h = C.c_void_p()
+        check(L.fwi_psv_create(C.byref(d), device, C.byref(h)), "fwi_psv_create")
+        self.h = h
+        self._last_nshots = 0
+        if set_model and problem.lam is not None:
+            self.set_model_lmr(problem.lam, problem.mu, problem.rho)
+        self.set_sources(problem.src_x, problem.src_z, problem.src_comp, problem.src_shot,
+                         problem.src_signal)
+        self.set_receivers(problem.rec_x, problem.rec_z, problem.rec_comp, problem.rec_shot)
+        self.set_fwi(problem.fwi_dt, problem.fwi_dx, problem.fwi_dz, problem.x1, problem.x2,
+                     problem.z1, problem.z2)
+
+    # ---- configuration ---------------------------------------------------------
+    def set_model(self, lam, mu, mu_zx, rho_zp, rho_xp):
+        a = [_f64(x) for x in (lam, mu, mu_zx, rho_zp, rho_xp)]
+        check(_capi.lib().fwi_psv_set_model(self.h, *[pd(x) for x in a]), "set_model")
+
+    def set_model_lmr(self, lam, mu, rho):
+        a = [_f64(x) for x in (lam, mu, rho)]
+        check(_capi.lib().fwi_psv_set_model_lmr(self.h, *[pd(x) for x in a]), "set_model_lmr")
+
+    def set_sources(self, x, z, comp, shot, signal):
+        x, z, comp, shot = map(_i32, (x, z, comp, shot))
+        sig = _f64(signal) if len(x) else np.zeros((1, self.p.nt))
+        check(_capi.lib().fwi_psv_set_sources(self.h, len(x), pi(x), pi(z), pi(comp), pi(shot),
+                                              pd(sig)), "set_sources")
+
+    def set_receivers(self, x, z, comp, shot):
+        x, z, comp, shot = map(_i32, (x, z, comp, shot))
+        self.nrec = len(x)
+        check(_capi.lib().fwi_psv_set_receivers(self.h, len(x), pi(x), pi(z), pi(comp), pi(shot)),
+              "set_receivers")
+
+    def set_fwi(self, fwi_dt=1, fwi_dx=1, fwi_dz=1, x1=0, x2=None, z1=0, z2=None):
+        x2 = self.p.nxt if x2 is None else x2
+        z2 = self.p.nzt if z2 is None else z2
+        check(_capi.lib().fwi_psv_set_fwi(self.h, fwi_dt, fwi_dx, fwi_dz, x1, x2, z1, z2), "set_fwi")
+        self.nfz = 1 + (z2 - z1) // fwi_dz
+        self.nfx = 1 + (x2 - x1) // fwi_dx
+
+    def set_strategy(self, strategy="full", snapshots=0, budget_bytes=0):
+        s = STRATEGIES[strategy] if isinstance(strategy, str) else int(strategy)
+        check(_capi.lib().fwi_psv_set_strategy(self.h, s, snapshots, budget_bytes), "set_strategy")
+
+    def set_exec(self, use_graphs=True, block_x=0, tile_z=0):
+        check(_capi.lib().fwi_psv_set_exec(self.h, int(use_graphs), block_x, tile_z), "set_exec")
+
+    def set_stream(self, stream_handle: int | None):
+        check(_capi.lib().fwi_psv_set_stream(self.h, C.c_void_p(stream_handle or 0)), "set_stream")
+
+    # ---- forward / backward -------------------------------------------------
+    def forward(self, shots, obs=None, keep=False, want_rec=True):
+        shots = _i32(np.atleast_1d(shots))
+        rec = np.zeros((max(self.nrec, 1), self.p.nt)) if want_rec else None
+        mis = np.zeros(len(shots))
+        o = _f64(obs) if obs is not None else None
+        check(_capi.lib().fwi_psv_forward(self.h, len(shots), pi(shots), pd(o), pd(rec), pd(mis),
+                                          int(keep)), "forward")
+        self._last_nshots = len(shots)
+        return rec, mis
+
+    def backward(self, sum_shots=False):
+        n = 1 if sum_shots else self._last_nshots
+        g = [np.zeros((n, self.nfz, self.nfx)) for _ in range(3)]
+        check(_capi.lib().fwi_psv_backward(self.h, *[pd(x) for x in g], int(sum_shots)), "backward")
+        if sum_shots:
+            g = [x[0] for x in g]
+        return tuple(g)
+
+    def energy(self, slot=0):
+        ws = np.zeros((self.p.nzt, self.p.nxt))
+        wr = np.zeros((self.p.nzt, self.p.nxt))
+        check(_capi.lib().fwi_psv_energy(self.h, slot, pd(ws), pd(wr)), "energy")
+        return ws, wr
+
+    def wavefield(self, which=0, slot=0):
+        f = [np.zeros((self.p.nzt, self.p.nxt)) for _ in range(5)]
+        check(_capi.lib().fwi_psv_wavefield(self.h, which, slot, *[pd(x) for x in f]), "wavefield")
+        return dict(zip(("vx", "vz", "sxx", "szx", "szz"), f))
+
+    def stats(self) -> dict:
+        s = _capi.Stats()
+        check(_capi.lib().fwi_psv_get_stats(self.h, C.byref(s)), "get_stats")
+        return {k: getattr(s, k) for k, _ in _capi.Stats._fields_}
+
+    def close(self):
+        if getattr(self, "h", None):
+            _capi.lib().fwi_psv_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()

@@ -1,0 +1,251 @@
+/*
+ * fwi_psv.h -- C ABI of the GB300 (sm_103a) engine for the 2-D elastic P-SV
+ * FWI hot path: staggered-grid stress/velocity time stepping with Holberg
+ * coefficients and CPML, source injection, seismogram recording, the adjoint
+ * pass and the lambda/mu/rho gradient.
+ *
+ * Replaces (reference = Mohammad-debug/CUDA_FWI, paths relative to its root):
+ *   forward_kernel_PSV_GPU / forward_kernel_PSV   CUDA_week2/fd_kernel.cuh:12-43, 75-120
+ *   adjoint_kernel_PSV_GPU / adjoint_kernel_PSV   CUDA_week2/fd_kernel.cuh:46-70, 123-173
+ * and the setup those calls depend on:
+ *   holbergcoeff                 CUDA_week2/holbergcoeff.cu:6
+ *   FDCpml::cpml_pro             CUDA_week2/fd_cpml.cu:59
+ *   FDMedium::average_parameters CUDA_week2/fd_medium.cu:128
+ *   create_wavelet               CUDA_week2/fd_seismogram.cu:166
+ *   FDGrid::total_grid           CUDA_week2/fd_grid.cu:52
+ *   calculate_l2_adjoint_sources CUDA_week2/fd_wave_model.cu:972
+ *
+ * Conventions
+ *   - Every call returns an int status (FWI_OK = 0 or a negative FWI_ERR_*);
+ *     nothing here calls exit().  fwi_psv_strerror() names a status and
+ *     fwi_psv_last_error() gives the detail message of the calling thread.
+ *   - Host arrays are FP64, row-major, in the reference's layouts:
+ *       wavefield, lam, mu, rho ........ [nzt][nxt]
+ *       mu_zx, rho_zp, rho_xp ........... [nzt-1][nxt-1]
+ *       CPML profiles a,b,K,a_half,.. .. [2*(npml+1)]
+ *       CPML x-strip memory ............. [nzt][2*(npml+1)]
+ *       CPML z-strip memory ............. [2*(npml+1)][nxt]
+ *       signals, seismograms ............ [nseis][nt]
+ *       FWI storage ..................... [nft][nfz][nfx]
+ *       gradients ....................... [nfz][nfx]
+ *     Grid indices (source/receiver x,z, FWI window) are padded-grid indices,
+ *     as after FDSeismogram::grid_adjustment / FDFWI::parse_configuration.
+ *   - The device computes in FP32.  An engine owns its device memory, is
+ *     bound to one device and one CUDA stream, and is not thread-safe; use one
+ *     engine per host thread.
+ */
+#ifndef FWI_PSV_H
+#define FWI_PSV_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FWI_PSV_ABI_VERSION 1
+
+enum {
+    FWI_OK = 0,
+    FWI_ERR_INVALID = -1,     /* bad argument, size or index */
+    FWI_ERR_UNSUPPORTED = -2, /* valid for the reference but outside this engine */
+    FWI_ERR_NOMEM = -3,       /* device or host allocation failed / over budget */
+    FWI_ERR_CUDA = -4,        /* CUDA runtime error (detail in fwi_psv_last_error) */
+    FWI_ERR_STATE = -5,       /* call out of order (e.g. backward before forward) */
+    FWI_ERR_DIVERGED = -6,    /* |syn-obs| > 1e10, where the reference exits */
+    FWI_ERR_NOFORWARD = -7,   /* backward without a retained forward */
+    FWI_ERR_NODEVICE = -8     /* no CUDA device / driver */
+};
+
+/* ---- setup helpers (host) ---------------------------------------------- */
+
+int fwi_psv_abi_version(void);
+const char* fwi_psv_strerror(int status);
+const char* fwi_psv_last_error(void);
+
+/* holbergcoeff.cu:6-60: hc[0..6] for fdorder 2..12 and max_rel_err 0..4. */
+int fwi_psv_holberg(int fdorder, int max_rel_err, double hc[7]);
+
+/* fd_cpml.cu:59-192: six profiles of length 2*(npml+1). */
+int fwi_psv_cpml_profile(int npml, double dh, double fpml, double npower, double k_max_pml,
+                         double rcoef, double damp_v_pml, double dt, double* a, double* b,
+                         double* K, double* a_half, double* b_half, double* K_half);
+
+/* fd_grid.cu:52-71 */
+int fwi_psv_total_grid(int nx, int nz, int fdorder, int npml, int fsurf, int* fpad, int* ppad,
+                       int* nxt, int* nzt);
+
+/* fd_seismogram.cu:166-185 (shape 1 = Ricker). */
+int fwi_psv_wavelet(double* signal, int nt, double dt, double amp, double fc, double ts,
+                    int shape);
+
+/* fd_medium.cu:128-159 on the host (FP64); outputs [nzt-1][nxt-1]. */
+int fwi_psv_average_parameters(int nzt, int nxt, const double* mu, const double* rho,
+                               double* mu_zx, double* rho_zp, double* rho_xp);
+
+/* ---- engine ------------------------------------------------------------ */
+
+typedef struct fwi_psv_engine fwi_psv_engine;
+
+/* Geometry and scheme: the leading scalar arguments of forward_kernel_PSV
+ * (fd_kernel.cuh:12-17) plus the CPML profiles (FDCpml::a..K_half). */
+typedef struct fwi_psv_desc {
+    int nt, nzt, nxt, fpad, ppad, npml, fsurf, fdorder;
+    double dt, dx, dz;
+    double hc[7];
+    const double *a, *b, *K, *a_half, *b_half, *K_half;
+} fwi_psv_desc;
+
+/* Gradient strategies (what the adjoint reads the forward wavefield from). */
+enum {
+    FWI_STORE_FULL = 0,     /* every sampled step kept in HBM (the reference's FDFWI storage) */
+    FWI_STORE_BINOMIAL = 1, /* binomial checkpointing with forward recompute */
+    FWI_STORE_RANDOM = 2    /* random-boundary wavefield reconstruction (no CPML on the source side) */
+};
+
+/* Gradient formula. */
+enum {
+    FWI_GRAD_REFERENCE = 0, /* the reference's correlation kernel (adjoint_kernel_PSV_GPU.cu:830-863) */
+    FWI_GRAD_EXACT = 1      /* discrete adjoint of the FP32 scheme (matches finite differences) */
+};
+
+/* Create an engine on CUDA device `device`.  The descriptor is copied. */
+int fwi_psv_create(const fwi_psv_desc* desc, int device, fwi_psv_engine** out);
+int fwi_psv_destroy(fwi_psv_engine* e);
+
+/* All work of the engine is queued on this stream (a cudaStream_t; NULL = the
+ * engine's own non-blocking stream). */
+int fwi_psv_set_stream(fwi_psv_engine* e, void* cuda_stream);
+
+/* Materials, reference layouts (fd_medium.cuh: lam, mu [nzt][nxt]; mu_zx,
+ * rho_zp, rho_xp [nzt-1][nxt-1]), as passed to forward_kernel_PSV. */
+int fwi_psv_set_model(fwi_psv_engine* e, const double* lam, const double* mu,
+                      const double* mu_zx, const double* rho_zp, const double* rho_xp);
+
+/* lam, mu, rho [nzt][nxt]; the staggered averages are formed on the device
+ * (FDMedium::average_parameters as a kernel). */
+int fwi_psv_set_model_lmr(fwi_psv_engine* e, const double* lam, const double* mu,
+                          const double* rho);
+
+/* Sources: FDSeismogram source arrays (x, z padded; comp 2 = vz, the only
+ * component the reference implements; shot = shot_to_fire) and their signals
+ * [nsrc][nt]. */
+int fwi_psv_set_sources(fwi_psv_engine* e, int nsrc, const int* x, const int* z,
+                        const int* comp, const int* shot, const double* signal);
+
+/* Receivers: the receiver FDSeismogram arrays (shot = receiver_to_record_shot). */
+int fwi_psv_set_receivers(fwi_psv_engine* e, int nrec, const int* x, const int* z,
+                          const int* comp, const int* shot);
+
+/* FWI sub-sampling and window ([full_waveform_inversion] after padding,
+ * fd_fwi.cu:28-51).  Defaults: 1,1,1 and the whole padded grid. */
+int fwi_psv_set_fwi(fwi_psv_engine* e, int fwi_dt, int fwi_dx, int fwi_dz, int x1, int x2,
+                    int z1, int z2);
+
+/* strategy = FWI_STORE_*; snapshots = checkpoint slots per shot for
+ * FWI_STORE_BINOMIAL (0 = as many as budget_bytes allows); budget_bytes = cap
+ * on the engine's device memory (0 = 90% of free memory at the call). */
+int fwi_psv_set_strategy(fwi_psv_engine* e, int strategy, int snapshots, size_t budget_bytes);
+
+/* Gradient formula (FWI_GRAD_*). */
+int fwi_psv_set_gradient_mode(fwi_psv_engine* e, int mode);
+
+/* Forward pass for `nshots` shots (ids in `shots`) run together on the device.
+ *   obs      [nrec][nt] observed data, or NULL (no misfit, no backward).
+ *   rec_out  [nrec][nt] synthetic seismograms (rows of receivers recorded by
+ *            a shot of this batch are written, others untouched), or NULL.
+ *   misfit   [nshots] per-shot J = sum 0.5 dt (syn-obs)^2, or NULL.
+ *   keep     non-zero: retain what backward needs (storage or checkpoints).
+ */
+int fwi_psv_forward(fwi_psv_engine* e, int nshots, const int* shots, const double* obs,
+                    double* rec_out, double* misfit, int keep);
+
+/* Backward for the batch of the last forward(keep=1): adjoint pass driven by
+ * the residual at the receivers, gradient accumulation.  Gradients are
+ * [nfz][nfx]; with sum_shots != 0 one summed triple is written, otherwise
+ * nshots consecutive triples ([nshots][nfz][nfx] each).  Any output may be NULL. */
+int fwi_psv_backward(fwi_psv_engine* e, double* grad_lam, double* grad_mu, double* grad_rho,
+                     int sum_shots);
+
+/* Energy sums of the last forward (Ws) and backward (Wr) for shot slot `slot`
+ * of the batch, [nzt][nxt] (the reference's We arrays). */
+int fwi_psv_energy(fwi_psv_engine* e, int slot, double* Ws, double* Wr);
+
+/* Final wavefield (vx, vz, sxx, szx, szz [nzt][nxt]) of batch slot `slot` after
+ * the last forward (which=0) or backward (which=1). */
+int fwi_psv_wavefield(fwi_psv_engine* e, int which, int slot, double* vx, double* vz,
+                      double* sxx, double* szx, double* szz);
+
+/* Counters of the last forward/backward: kernel launches, time steps
+ * advanced (forward + recompute), adjoint steps, and device bytes held. */
+typedef struct fwi_psv_stats {
+    int64_t launches, forward_steps, recompute_steps, adjoint_steps;
+    int64_t device_bytes, snapshots;
+    double last_forward_ms, last_backward_ms;
+} fwi_psv_stats;
+int fwi_psv_get_stats(fwi_psv_engine* e, fwi_psv_stats* out);
+
+/* The binomial checkpoint schedule behind FWI_STORE_BINOMIAL (Griewank &
+ * Walther's revolve bound) for reversing `nsteps` super-steps (fwi_dt time
+ * steps each) with `slots` checkpoint slots.  actions is [cap][3] of
+ * (kind, a, b): 0 = advance state a -> b, 1 = save state b into slot a,
+ * 2 = restore slot a (-1 = the zero initial state) holding state b,
+ * 3 = adjoint of super-step a.  *count = actions written (FWI_ERR_INVALID if
+ * cap is too small, with *count = actions needed); *forward_steps = advance cost. */
+int fwi_psv_checkpoint_plan(int nsteps, int slots, int* actions, int cap, int* count,
+                            long long* forward_steps);
+
+/* Execution options: use_graphs != 0 captures the time loop in CUDA graphs
+ * (default 1); block_x / tile_z override the autotuned tile (0 = auto). */
+int fwi_psv_set_exec(fwi_psv_engine* e, int use_graphs, int block_x, int tile_z);
+
+/* ---- reference-shaped calls --------------------------------------------- */
+
+/* forward_kernel_PSV (fd_kernel.cuh:12-43) with flat FP64 host arrays in the
+ * reference layouts: resets the state, runs nt steps on the device and writes
+ * back the final wavefield, We, the CPML memory, rec_signal rows of `ishot`
+ * and, when fwinv, the FWI storage (fwi_vx .. fwi_szz, [nft][nfz][nfx]). */
+int fwi_psv_forward_kernel(int ishot, int nt, int nzt, int nxt, int fpad, int ppad, double dt,
+                           double dx, double dz, int snap_interval, int fsurf, const double* hc,
+                           int fdorder, double* vx, double* vz, double* sxx, double* szx,
+                           double* szz, double* We, const double* lam, const double* mu,
+                           const double* mu_zx, const double* rho_zp, const double* rho_xp,
+                           int npml, const double* a, const double* b, const double* K,
+                           const double* a_half, const double* b_half, const double* K_half,
+                           double* mem_vx_x, double* mem_vx_z, double* mem_vz_x,
+                           double* mem_vz_z, double* mem_sxx_x, double* mem_szx_x,
+                           double* mem_szz_z, double* mem_szx_z, int nsrc, const int* src_x,
+                           const int* src_z, const int* src_comp, const double* src_signal,
+                           const int* source_to_fire_shot, int nrec, const int* rec_x,
+                           const int* rec_z, const int* rec_comp, double* rec_signal,
+                           const int* receiver_to_record_shot, int fwinv, int fwi_dt,
+                           int fwi_dx, int fwi_dz, int fwi_x1, int fwi_x2, int fwi_z1,
+                           int fwi_z2, double* fwi_vx, double* fwi_vz, double* fwi_sxx,
+                           double* fwi_szx, double* fwi_szz);
+
+/* adjoint_kernel_PSV (fd_kernel.cuh:46-70): reverse-time pass injecting
+ * src_signal (the residual) at the src positions, gradient from the FWI
+ * storage written by fwi_psv_forward_kernel.  Writes grad_lam/mu/rho, the
+ * final adjoint wavefield, We and the CPML memory. */
+int fwi_psv_adjoint_kernel(int ishot, int nt, int nzt, int nxt, int fpad, int ppad, double dt,
+                           double dx, double dz, int snap_interval, int fsurf, const double* hc,
+                           int fdorder, double* vx, double* vz, double* sxx, double* szx,
+                           double* szz, double* We, const double* lam, const double* mu,
+                           const double* mu_zx, const double* rho_zp, const double* rho_xp,
+                           int npml, const double* a, const double* b, const double* K,
+                           const double* a_half, const double* b_half, const double* K_half,
+                           double* mem_vx_x, double* mem_vx_z, double* mem_vz_x,
+                           double* mem_vz_z, double* mem_sxx_x, double* mem_szx_x,
+                           double* mem_szz_z, double* mem_szx_z, int nsrc, const int* src_x,
+                           const int* src_z, const int* src_comp, const double* src_signal,
+                           const int* source_to_fire_shot, int fwinv, int fwi_dt, int fwi_dx,
+                           int fwi_dz, int fwi_x1, int fwi_x2, int fwi_z1, int fwi_z2,
+                           const double* fwi_vx, const double* fwi_vz, const double* fwi_sxx,
+                           const double* fwi_szx, const double* fwi_szz, double* grad_lam,
+                           double* grad_mu, double* grad_rho);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FWI_PSV_H */

@@ -1,0 +1,541 @@
+/*
+ * fwi_oracle.c -- FP64 CPU restatement of the reference's FWI hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY (the parity oracle); see fwi_oracle.h for the
+ * scope, the generalisation to orders 4..12 and the reference line map.
+ * Compile with -ffp-contract=off so that x86-64 and aarch64 round alike and
+ * fdorder-2 results match the reference's own CPU functions bit for bit.
+ */
+#include "fwi_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <stddef.h>
+#include <string.h>
+
+#define IX2(p, iz, ix, pitch) (p)[(size_t)(iz) * (size_t)(pitch) + (size_t)(ix)]
+
+int orc_nft(int nt, int fwi_dt) { return 1 + (nt - 1) / fwi_dt; }
+int orc_nfz(const orc_fwi* f) { return 1 + (f->z2 - f->z1) / f->fwi_dz; }
+int orc_nfx(const orc_fwi* f) { return 1 + (f->x2 - f->x1) / f->fwi_dx; }
+
+/* Holberg (1987) optimised staggered-grid coefficients, rows = maximum relative
+ * group-velocity error index 0..4 (0 = Taylor), columns = order 2..12; entry 0
+ * of each row is the table's accuracy figure, entries 1..6 the coefficients.
+ * Same table as CUDA_week2/holbergcoeff.cu:10-52 (published values). */
+static const double k_holberg[5][6][7] = {
+    {{23.0, 1.0, 0.0, 0.0, 0.0, 0.0, 0.0},
+     {8.0, 9.0 / 8.0, -1.0 / 24.0, 0.0, 0.0, 0.0, 0.0},
+     {6.0, 75.0 / 64.0, -25.0 / 384.0, 3.0 / 640.0, 0.0, 0.0, 0.0},
+     {5.0, 1225.0 / 1024.0, -245.0 / 3072.0, 49.0 / 5120.0, -5.0 / 7168.0, 0.0, 0.0},
+     {5.0, 19845.0 / 16384.0, -735.0 / 8192.0, 567.0 / 40960.0, -405.0 / 229376.0,
+      35.0 / 294912.0, 0.0},
+     {4.0, 160083.0 / 131072.0, -12705.0 / 131072.0, 22869.0 / 1310720.0,
+      -5445.0 / 1835008.0, 847.0 / 2359296.0, -63.0 / 2883584.0}},
+    {{49.7, 1.0010, 0.0, 0.0, 0.0, 0.0, 0.0},
+     {8.32, 1.1382, -0.046414, 0.0, 0.0, 0.0, 0.0},
+     {4.77, 1.1965, -0.078804, 0.0081781, 0.0, 0.0, 0.0},
+     {3.69, 1.2257, -0.099537, 0.018063, -0.0026274, 0.0, 0.0},
+     {3.19, 1.2415, -0.11231, 0.026191, -0.0064682, 0.001191, 0.0},
+     {2.91, 1.2508, -0.12034, 0.032131, -0.010142, 0.0029857, -0.00066667}},
+    {{22.2, 1.0050, 0.0, 0.0, 0.0, 0.0, 0.0},
+     {5.65, 1.1534, -0.052806, 0.0, 0.0, 0.0, 0.0},
+     {3.74, 1.2111, -0.088313, 0.011768, 0.0, 0.0, 0.0},
+     {3.11, 1.2367, -0.10815, 0.023113, -0.0046905, 0.0, 0.0},
+     {2.80, 1.2496, -0.11921, 0.031130, -0.0093272, 0.0025161, 0.0},
+     {2.62, 1.2568, -0.12573, 0.036423, -0.013132, 0.0047484, -0.0015979}},
+    {{15.8, 1.0100, 0.0, 0.0, 0.0, 0.0, 0.0},
+     {4.80, 1.1640, -0.057991, 0.0, 0.0, 0.0, 0.0},
+     {3.39, 1.2192, -0.094070, 0.014608, 0.0, 0.0, 0.0},
+     {2.90, 1.2422, -0.11269, 0.026140, -0.0064054, 0.0, 0.0},
+     {2.65, 1.2534, -0.12257, 0.033755, -0.011081, 0.0036784, 0.0},
+     {2.51, 1.2596, -0.12825, 0.038550, -0.014763, 0.0058619, -0.0024538}},
+    {{9.16, 1.0300, 0.0, 0.0, 0.0, 0.0, 0.0},
+     {3.47, 1.1876, -0.072518, 0.0, 0.0, 0.0, 0.0},
+     {2.91, 1.2341, -0.10569, 0.022589, 0.0, 0.0, 0.0},
+     {2.61, 1.2516, -0.12085, 0.032236, -0.011459, 0.0, 0.0},
+     {2.45, 1.2596, -0.12829, 0.038533, -0.014681, 0.0072580, 0.0},
+     {2.36, 1.2640, -0.13239, 0.042217, -0.017803, 0.0081959, -0.0051848}},
+};
+
+int orc_holberg(int fdorder, int max_rel_err, double hc[7]) {
+    int nl = fdorder / 2 - 1;
+    if (fdorder < 2 || fdorder > 12 || (fdorder & 1) || max_rel_err < 0 || max_rel_err > 4)
+        return -1;
+    for (int i = 0; i < 7; i++) hc[i] = k_holberg[max_rel_err][nl][i];
+    return 0;
+}
+
+/* One side of the CPML profile at abscissa `dist` (metres into the layer, <0 = outside).
+ * Writes d, K, alpha following the formulas of fd_cpml.cu:95-110. */
+static void cpml_point(double dist, double thickness, double d0, double npower, double kmax,
+                       double alpha_max, double* d, double* K, double* alpha) {
+    *d = 0.0;
+    *alpha = 0.0;
+    if (dist >= 0) {
+        double xn = dist / thickness;
+        *d = d0 * pow(xn, npower);
+        *K = 1.0 + (kmax - 1.0) * pow(xn, npower);
+        *alpha = alpha_max * (1.0 - xn);
+    }
+    if (*alpha < 0.0) *alpha = 0.0;
+}
+
+static void cpml_ab(double d, double K, double alpha, double dt, double* a, double* b) {
+    *b = exp(-(d / K + alpha) * dt);
+    if (fabs(d) > 1.0e-6) *a = d * (*b - 1.0) / (K * (d + K * alpha));
+}
+
+void orc_cpml(int npml, double dh, double fpml, double npower, double k_max_pml, double rcoef,
+              double damp_v_pml, double dt, double* a, double* b, double* K, double* a_half,
+              double* b_half, double* K_half) {
+    const double alpha_max = 2.0 * ORC_PI * (fpml / 2.0);
+    const double thick = npml * dh;
+    const double d0 = -(npower + 1) * damp_v_pml * log(rcoef) / (2.0 * thick);
+    const int n = 2 * (npml + 1);
+    for (int i = 0; i < n; i++) {
+        a[i] = 0.0; a_half[i] = 0.0;
+        b[i] = 1.0; b_half[i] = 1.0;
+        K[i] = 1.0; K_half[i] = 1.0;
+    }
+    for (int i = 0; i < n; i++) {
+        double x = dh * (double)i, dist, dist_h;
+        if (i <= npml) { /* left: measured from the outer edge inwards */
+            dist = thick - x;
+            dist_h = thick - (x + dh / 2.0);
+        } else { /* right: measured from dh*(npml+1) outwards */
+            dist = x - dh * (npml + 1);
+            dist_h = (x + dh / 2.0) - dh * (npml + 1);
+        }
+        double d, al, dhf, alh;
+        cpml_point(dist, thick, d0, npower, k_max_pml, alpha_max, &d, &K[i], &al);
+        cpml_point(dist_h, thick, d0, npower, k_max_pml, alpha_max, &dhf, &K_half[i], &alh);
+        cpml_ab(d, K[i], al, dt, &a[i], &b[i]);
+        cpml_ab(dhf, K_half[i], alh, dt, &a_half[i], &b_half[i]);
+    }
+}
+
+void orc_average(int nzt, int nxt, const double* lam, const double* mu, const double* rho,
+                 double* mu_zx, double* rho_zp, double* rho_xp) {
+    (void)lam;
+    const int dz = nzt - 1, dx = nxt - 1;
+    for (int ix = 0; ix < dx; ix++) {
+        for (int iz = 0; iz < dz; iz++) {
+            double m00 = IX2(mu, iz, ix, nxt), m01 = IX2(mu, iz, ix + 1, nxt);
+            double m10 = IX2(mu, iz + 1, ix, nxt), m11 = IX2(mu, iz + 1, ix + 1, nxt);
+            double h = 4.0 / ((1.0 / m00) + (1.0 / m01) + (1.0 / m10) + (1.0 / m11));
+            if (m00 == 0.0 || m01 == 0.0 || m10 == 0.0 || m11 == 0.0) h = 0.0;
+            IX2(mu_zx, iz, ix, dx) = h;
+            double r00 = IX2(rho, iz, ix, nxt), r10 = IX2(rho, iz + 1, ix, nxt);
+            double r01 = IX2(rho, iz, ix + 1, nxt);
+            IX2(rho_zp, iz, ix, dx) = 1.0 / (0.5 * (r00 + r10));
+            IX2(rho_xp, iz, ix, dx) = 1.0 / (0.5 * (r00 + r01));
+            if (r00 < 1e-4 && r10 < 1e-4) IX2(rho_zp, iz, ix, dx) = 0.0;
+            /* the reference's second guard also writes rho_zp (fd_medium.cu:152-154) */
+            if (r00 < 1e-4 && r01 < 1e-4) IX2(rho_zp, iz, ix, dx) = 0.0;
+        }
+    }
+}
+
+void orc_wavelet(double* signal, int nt, double dt, double amp, double fc, double ts, int shape) {
+    const double fci = 1.0 / fc;
+    if (shape != 1) return;
+    for (int it = 0; it < nt; it++) {
+        double t = it * dt;
+        double tau = ORC_PI * (t - 1.5 * fci - ts) / (1.5 * fci);
+        signal[it] = amp * (1.0 - 2.0 * tau * tau) * exp(-2.0 * tau * tau);
+    }
+}
+
+void orc_total_grid(int nx, int nz, int fdorder, int npml, int fsurf, int* fpad, int* ppad,
+                    int* nxt, int* nzt) {
+    *fpad = fdorder / 2;
+    *ppad = npml + *fpad;
+    *nxt = nx + 2 * *ppad;
+    *nzt = fsurf ? nz + *ppad + *fpad : nz + 2 * *ppad;
+}
+
+/* ---------------------------------------------------------------------------
+ * Stencils.  Evaluation order mirrors the reference at fdorder 2:
+ *   d = (dxi*hc[1]) * (f[i] - f[i-1]).
+ * ------------------------------------------------------------------------- */
+static inline double dminus(const double* f, ptrdiff_t c, ptrdiff_t s, int fpad, const double* hd) {
+    double acc = 0.0;
+    for (int k = 1; k <= fpad; k++) acc += hd[k] * (f[c + (k - 1) * s] - f[c - k * s]);
+    return acc;
+}
+static inline double dplus(const double* f, ptrdiff_t c, ptrdiff_t s, int fpad, const double* hd) {
+    double acc = 0.0;
+    for (int k = 1; k <= fpad; k++) acc += hd[k] * (f[c + k * s] - f[c - (k - 1) * s]);
+    return acc;
+}
+
+/* Bottom CPML index offset.  fdorder 2 is the reference's (forward_kernel_PSV_GPU.cu:749-755);
+ * with a free surface at higher orders the reference's formula would index past
+ * 2(npml+1), so the offset is chosen to keep the same layer cells on indices npml+1..2npml+1. */
+static int bottom_offset(const orc_grid* g) {
+    if (g->fsurf) return g->nzt - 2 * g->ppad + g->fpad - 2;
+    return g->nzt - 2 * g->ppad + g->fpad - 1;
+}
+
+/* One stress update (forward_kernel_PSV_GPU.cu:830-931) and the mirror (:934-942). */
+static void stress_pass(const orc_grid* g, const orc_medium* m, orc_wave* w) {
+    const int nxt = g->nxt, nzt = g->nzt, fpad = g->fpad, ppad = g->ppad, npml = g->npml;
+    const int tp = 2 * (npml + 1);
+    const int pnx = nxt - 2 * ppad + fpad - 1, pnz = bottom_offset(g);
+    const double dxi = 1.0 / g->dx, dzi = 1.0 / g->dz, dt = g->dt;
+    double hx[7], hz[7];
+    for (int k = 1; k <= fpad; k++) { hx[k] = dxi * g->hc[k]; hz[k] = dzi * g->hc[k]; }
+    const int nz1 = fpad, nz2 = nzt - fpad, nx1 = fpad, nx2 = nxt - fpad;
+    for (int iz = nz1; iz < nz2; iz++) {
+        for (int ix = nx1; ix < nx2; ix++) {
+            size_t c = (size_t)iz * nxt + ix;
+            double vx_x = dminus(w->vx, c, 1, fpad, hx);
+            double vz_x = dplus(w->vz, c, 1, fpad, hx);
+            double vx_z = dplus(w->vx, c, nxt, fpad, hz);
+            double vz_z = dminus(w->vz, c, nxt, fpad, hz);
+            if (npml > 0) {
+                int px = -1;
+                if (ix >= fpad && ix <= ppad) px = ix - fpad;
+                if (px >= 0) {
+                    double* mx = &IX2(w->mem_vx_x, iz, px, tp);
+                    double* mz = &IX2(w->mem_vz_x, iz, px, tp);
+                    *mx = g->b[px] * *mx + g->a[px] * vx_x;
+                    *mz = g->b_half[px] * *mz + g->a_half[px] * vz_x;
+                    vx_x = vx_x / g->K[px] + *mx;
+                    vz_x = vz_x / g->K_half[px] + *mz;
+                }
+                if (ix >= (nxt - ppad - 1) && ix < nxt - fpad) {
+                    px = ix - pnx;
+                    double* mx = &IX2(w->mem_vx_x, iz, px, tp);
+                    double* mz = &IX2(w->mem_vz_x, iz, px, tp);
+                    *mx = g->b[px] * *mx + g->a[px] * vx_x;
+                    *mz = g->b_half[px] * *mz + g->a_half[px] * vz_x;
+                    vx_x = vx_x / g->K[px] + *mx;
+                    vz_x = vz_x / g->K_half[px] + *mz;
+                }
+                if (iz >= fpad && iz <= ppad && !g->fsurf) {
+                    int pz = iz - fpad;
+                    double* mz = &IX2(w->mem_vz_z, pz, ix, nxt);
+                    double* mx = &IX2(w->mem_vx_z, pz, ix, nxt);
+                    *mz = g->b[pz] * *mz + g->a[pz] * vz_z;
+                    *mx = g->b_half[pz] * *mx + g->a_half[pz] * vx_z;
+                    vz_z = vz_z / g->K[pz] + *mz;
+                    vx_z = vx_z / g->K_half[pz] + *mx;
+                }
+                if (iz >= (nzt - ppad - 1) && iz < nzt - fpad) {
+                    int pz = iz - pnz;
+                    double* mz = &IX2(w->mem_vz_z, pz, ix, nxt);
+                    double* mx = &IX2(w->mem_vx_z, pz, ix, nxt);
+                    *mz = g->b[pz] * *mz + g->a[pz] * vz_z;
+                    *mx = g->b_half[pz] * *mx + g->a_half[pz] * vx_z;
+                    vz_z = vz_z / g->K[pz] + *mz;
+                    vx_z = vx_z / g->K_half[pz] + *mx;
+                }
+            }
+            const double lam = m->lam[c], mu = m->mu[c];
+            const double muzx = IX2(m->mu_zx, iz, ix, nxt - 1);
+            w->szx[c] += dt * muzx * (vz_x + vx_z);
+            w->sxx[c] += dt * (lam * (vx_x + vz_z) + (2.0 * mu * vx_x));
+            w->szz[c] += dt * (lam * (vx_x + vz_z) + (2.0 * mu * vz_z));
+            if (g->fsurf && iz == fpad) {
+                w->szz[c] = 0.0;
+                w->szx[c] = 0.0;
+                w->sxx[c] = 4.0 * dt * vx_x * (lam * mu + mu * mu) / (lam + 2.0 * mu);
+            }
+        }
+    }
+    if (g->fsurf) {
+        for (int ix = nx1; ix < nx2; ix++)
+            for (int sz = 1; sz <= fpad; sz++) {
+                IX2(w->szx, fpad - sz, ix, nxt) = -IX2(w->szx, fpad + sz, ix, nxt);
+                IX2(w->szz, fpad - sz, ix, nxt) = -IX2(w->szz, fpad + sz, ix, nxt);
+            }
+    }
+}
+
+/* One velocity update with energy accumulation (forward_kernel_PSV_GPU.cu:946-1023). */
+static void velocity_pass(const orc_grid* g, const orc_medium* m, orc_wave* w) {
+    const int nxt = g->nxt, nzt = g->nzt, fpad = g->fpad, ppad = g->ppad, npml = g->npml;
+    const int tp = 2 * (npml + 1);
+    const int pnx = nxt - 2 * ppad + fpad - 1, pnz = bottom_offset(g);
+    const double dxi = 1.0 / g->dx, dzi = 1.0 / g->dz, dt = g->dt;
+    double hx[7], hz[7];
+    for (int k = 1; k <= fpad; k++) { hx[k] = dxi * g->hc[k]; hz[k] = dzi * g->hc[k]; }
+    const int nz1 = fpad, nz2 = nzt - fpad, nx1 = fpad, nx2 = nxt - fpad;
+    for (int iz = nz1; iz < nz2; iz++) {
+        for (int ix = nx1; ix < nx2; ix++) {
+            size_t c = (size_t)iz * nxt + ix;
+            double sxx_x = dplus(w->sxx, c, 1, fpad, hx);
+            double szx_x = dminus(w->szx, c, 1, fpad, hx);
+            double szx_z = dminus(w->szx, c, nxt, fpad, hz);
+            double szz_z = dplus(w->szz, c, nxt, fpad, hz);
+            if (npml > 0) {
+                if (ix >= fpad && ix < ppad) {
+                    int px = ix - fpad;
+                    double* mx = &IX2(w->mem_sxx_x, iz, px, tp);
+                    double* mz = &IX2(w->mem_szx_x, iz, px, tp);
+                    *mx = g->b[px] * *mx + g->a[px] * sxx_x;
+                    *mz = g->b_half[px] * *mz + g->a_half[px] * szx_x;
+                    sxx_x = sxx_x / g->K[px] + *mx;
+                    szx_x = szx_x / g->K_half[px] + *mz;
+                }
+                if (ix >= (nxt - ppad - 1) && ix < nxt - fpad) {
+                    int px = ix - pnx;
+                    double* mx = &IX2(w->mem_sxx_x, iz, px, tp);
+                    double* mz = &IX2(w->mem_szx_x, iz, px, tp);
+                    *mx = g->b[px] * *mx + g->a[px] * sxx_x;
+                    *mz = g->b_half[px] * *mz + g->a_half[px] * szx_x;
+                    sxx_x = sxx_x / g->K[px] + *mx;
+                    szx_x = szx_x / g->K_half[px] + *mz;
+                }
+                if (iz >= fpad && iz < ppad && !g->fsurf) {
+                    int pz = iz - fpad;
+                    double* mz = &IX2(w->mem_szz_z, pz, ix, nxt);
+                    double* mx = &IX2(w->mem_szx_z, pz, ix, nxt);
+                    *mz = g->b[pz] * *mz + g->a[pz] * szz_z;
+                    *mx = g->b_half[pz] * *mx + g->a_half[pz] * szx_z;
+                    szz_z = szz_z / g->K[pz] + *mz;
+                    szx_z = szx_z / g->K_half[pz] + *mx;
+                }
+                if (iz >= (nzt - ppad - 1) && iz < nzt - fpad) {
+                    int pz = iz - pnz;
+                    double* mz = &IX2(w->mem_szz_z, pz, ix, nxt);
+                    double* mx = &IX2(w->mem_szx_z, pz, ix, nxt);
+                    *mz = g->b[pz] * *mz + g->a[pz] * szz_z;
+                    *mx = g->b_half[pz] * *mx + g->a_half[pz] * szx_z;
+                    szz_z = szz_z / g->K[pz] + *mz;
+                    szx_z = szx_z / g->K_half[pz] + *mx;
+                }
+            }
+            const double rxp = IX2(m->rho_xp, iz, ix, nxt - 1);
+            const double rzp = IX2(m->rho_zp, iz, ix, nxt - 1);
+            w->vx[c] += dt * rxp * (sxx_x + szx_z);
+            w->vz[c] += dt * rzp * (szx_x + szz_z);
+            w->We[c] += w->vx[c] * w->vx[c] + w->vz[c] * w->vz[c];
+        }
+    }
+}
+
+static void reset_wave(const orc_grid* g, orc_wave* w) {
+    size_t n = (size_t)g->nzt * g->nxt;
+    size_t nxs = (size_t)g->nzt * 2 * (g->npml + 1), nzs = (size_t)2 * (g->npml + 1) * g->nxt;
+    memset(w->vx, 0, n * sizeof(double));
+    memset(w->vz, 0, n * sizeof(double));
+    memset(w->sxx, 0, n * sizeof(double));
+    memset(w->szx, 0, n * sizeof(double));
+    memset(w->szz, 0, n * sizeof(double));
+    memset(w->We, 0, n * sizeof(double));
+    /* the reference's driver resets the CPML memory before every pass
+     * (fd_wave_model.cu:781-785, 839-840); the oracle does it here */
+    memset(w->mem_vx_x, 0, nxs * sizeof(double));
+    memset(w->mem_vz_x, 0, nxs * sizeof(double));
+    memset(w->mem_sxx_x, 0, nxs * sizeof(double));
+    memset(w->mem_szx_x, 0, nxs * sizeof(double));
+    memset(w->mem_vx_z, 0, nzs * sizeof(double));
+    memset(w->mem_vz_z, 0, nzs * sizeof(double));
+    memset(w->mem_szz_z, 0, nzs * sizeof(double));
+    memset(w->mem_szx_z, 0, nzs * sizeof(double));
+}
+
+static int check_grid(const orc_grid* g) {
+    if (g->fdorder < 2 || g->fdorder > 12 || (g->fdorder & 1)) return -1;
+    if (g->fpad != g->fdorder / 2 || g->ppad != g->npml + g->fpad) return -2;
+    if (g->nt < 1 || g->nxt <= 2 * g->ppad || g->nzt <= 2 * g->fpad) return -3;
+    return 0;
+}
+
+int orc_forward(int ishot, const orc_grid* g, const orc_medium* m, orc_wave* w,
+                const orc_seis* src, const double* src_signal, const orc_seis* rec,
+                double* rec_signal, orc_fwi* f) {
+    int rc = check_grid(g);
+    if (rc) return rc;
+    const int nxt = g->nxt, nt = g->nt;
+    reset_wave(g, w);
+    int nft = 0, nfz = 0, nfx = 0;
+    if (f && f->fwinv) {
+        nft = orc_nft(nt, f->fwi_dt); nfz = orc_nfz(f); nfx = orc_nfx(f);
+        size_t ns = (size_t)nft * nfz * nfx;
+        memset(f->vx, 0, ns * sizeof(double)); memset(f->vz, 0, ns * sizeof(double));
+        memset(f->sxx, 0, ns * sizeof(double)); memset(f->szx, 0, ns * sizeof(double));
+        memset(f->szz, 0, ns * sizeof(double));
+    }
+    for (int it = 0; it < nt; it++) {
+        if (f && f->fwinv && !(it % f->fwi_dt)) {
+            int tf = it / f->fwi_dt;
+            for (int iz = f->z1; iz < f->z2; iz += f->fwi_dz) {
+                int zf = (iz - f->z1) / f->fwi_dz;
+                for (int ix = f->x1; ix < f->x2; ix += f->fwi_dx) {
+                    int xf = (ix - f->x1) / f->fwi_dx;
+                    size_t o = ((size_t)tf * nfz + zf) * nfx + xf, c = (size_t)iz * nxt + ix;
+                    f->sxx[o] = w->sxx[c];
+                    f->szx[o] = w->szx[c];
+                    f->szz[o] = w->szz[c];
+                    f->vx[o] = w->vx[c] / g->dt;
+                    f->vz[o] = w->vz[c] / g->dt;
+                }
+            }
+        }
+        stress_pass(g, m, w);
+        velocity_pass(g, m, w);
+        for (int is = 0; src && is < src->n; is++)
+            if (src->shot[is] == ishot && src->comp[is] == 2)
+                IX2(w->vz, src->z[is], src->x[is], nxt) += src_signal[(size_t)is * nt + it];
+        for (int ir = 0; rec && ir < rec->n; ir++)
+            if (rec->shot[ir] == ishot && rec->comp[ir] == 2)
+                rec_signal[(size_t)ir * nt + it] = IX2(w->vz, rec->z[ir], rec->x[ir], nxt);
+    }
+    return 0;
+}
+
+int orc_adjoint(int ishot, const orc_grid* g, const orc_medium* m, orc_wave* w,
+                const orc_seis* adj, const double* adj_signal, const orc_fwi* f,
+                double* grad_lam, double* grad_mu, double* grad_rho) {
+    int rc = check_grid(g);
+    if (rc) return rc;
+    const int nxt = g->nxt, nzt = g->nzt, nt = g->nt, fpad = g->fpad;
+    const double dt = g->dt;
+    reset_wave(g, w);
+    size_t n = (size_t)nzt * nxt;
+    double* ux = (double*)calloc(n, sizeof(double));
+    double* uz = (double*)calloc(n, sizeof(double));
+    if (!ux || !uz) { free(ux); free(uz); return -4; }
+    const int nfz = orc_nfz(f), nfx = orc_nfx(f);
+    memset(grad_lam, 0, (size_t)nfz * nfx * sizeof(double));
+    memset(grad_mu, 0, (size_t)nfz * nfx * sizeof(double));
+    memset(grad_rho, 0, (size_t)nfz * nfx * sizeof(double));
+    for (int it = nt - 1; it >= 0; it--) {
+        for (int iz = fpad; iz < nzt - fpad; iz++)
+            for (int ix = fpad; ix < nxt - fpad; ix++) {
+                size_t c = (size_t)iz * nxt + ix;
+                uz[c] += dt * w->vz[c];
+                ux[c] += dt * w->vx[c];
+            }
+        if (f->fwinv && !(it % f->fwi_dt)) {
+            int tf = it / f->fwi_dt;
+            for (int iz = f->z1; iz < f->z2; iz += f->fwi_dz) {
+                int zf = (iz - f->z1) / f->fwi_dz;
+                for (int ix = f->x1; ix < f->x2; ix += f->fwi_dx) {
+                    int xf = (ix - f->x1) / f->fwi_dx;
+                    size_t o = ((size_t)tf * nfz + zf) * nfx + xf, c = (size_t)iz * nxt + ix;
+                    size_t gi = (size_t)zf * nfx + xf;
+                    double lam = m->lam[c], mu = m->mu[c];
+                    double s1 = (f->sxx[o] + f->szz[o]) * (w->sxx[c] + w->szz[c]) * 0.25 /
+                                ((lam + mu) * (lam + mu));
+                    double s2 = (f->sxx[o] - f->szz[o]) * (w->sxx[c] - w->szz[c]) / (mu * mu);
+                    double s3 = (f->szx[o] * w->szx[c]) / (mu * mu);
+                    double s4 = ux[c] * f->vx[o] + uz[c] * f->vz[o];
+                    grad_lam[gi] += f->fwi_dt * dt * s1;
+                    grad_mu[gi] += f->fwi_dt * dt * (s3 + s1 + s2);
+                    grad_rho[gi] -= f->fwi_dt * dt * s4;
+                }
+            }
+        }
+        stress_pass(g, m, w);
+        velocity_pass(g, m, w);
+        for (int is = 0; adj && is < adj->n; is++)
+            if (adj->shot[is] == ishot && adj->comp[is] == 2)
+                IX2(w->vz, adj->z[is], adj->x[is], nxt) += adj_signal[(size_t)is * nt + it];
+    }
+    free(ux);
+    free(uz);
+    return 0;
+}
+
+double orc_l2_adjoint_sources(int nr, int nt, double dt, double* signal, const double* signal_meas,
+                              int* blowup) {
+    double misfit = 0.0;
+    if (blowup) *blowup = 0;
+    for (int ir = 0; ir < nr; ir++)
+        for (int it = 0; it < nt; it++) {
+            size_t i = (size_t)ir * nt + it;
+            double diff = signal[i] - signal_meas[i];
+            misfit += 0.5 * dt * diff * diff;
+            signal[i] = diff;
+            if (fabs(diff) > 1.0e+10 && blowup) *blowup = 1;
+        }
+    return misfit;
+}
+
+void orc_medium_average(int nzt, int nxt, const double* lam, const double* mu, const double* rho,
+                        double* c_lam, double* c_mu, double* c_rho) {
+    double sl = 0.0, sm = 0.0, sr = 0.0;
+    for (int iz = 0; iz < nzt; iz++)
+        for (int ix = 0; ix < nxt; ix++) {
+            size_t c = (size_t)iz * nxt + ix;
+            sl += lam[c]; sm += mu[c]; sr += rho[c];
+        }
+    *c_lam = sl / (nzt * nxt);
+    *c_mu = sm / (nzt * nxt);
+    *c_rho = sr / (nzt * nxt);
+}
+
+void orc_scale_gradients(int nxt, const double* Ws, const double* Wr, double c_rho, double c_lam,
+                         double c_mu, int nz, int nx, int z1, int x1, int fdz, int fdx,
+                         int grad_pitch, double* grad_lam, double* grad_mu, double* grad_rho) {
+    const double eps = 0.005;
+    double wmax = 0.0;
+    for (int iz = z1; iz < nz; iz += fdz)
+        for (int ix = x1; ix < nx; ix += fdx) {
+            double we = sqrt(IX2(Ws, iz, ix, nxt) * IX2(Wr, iz, ix, nxt));
+            if (we > wmax) wmax = we;
+        }
+    for (int iz = z1; iz < nz; iz += fdz)
+        for (int ix = x1; ix < nx; ix += fdx) {
+            double we = sqrt(IX2(Ws, iz, ix, nxt) * IX2(Wr, iz, ix, nxt)) + eps * wmax;
+            size_t gi = (size_t)iz * grad_pitch + ix;
+            grad_lam[gi] = grad_lam[gi] / (we * c_lam * c_lam);
+            grad_mu[gi] = grad_mu[gi] / (we * c_mu * c_mu);
+            grad_rho[gi] = grad_rho[gi] / (we * c_rho * c_rho);
+        }
+}
+
+void orc_grad_update(double* mat, double* mat_new, const double* grad, int pitch, int gpitch,
+                     double step_length, int dimz, int dimx, int z1, int x1, int fwi_dz,
+                     int fwi_dx, int override_, int mat_type) {
+    double mat_max = 0.0, grad_max = 0.0, hi = 0.0, lo = 0.0;
+    if (mat_type == 1) { hi = 3000; lo = 1.5; }
+    else if (mat_type == 2) { hi = 48.0e+9; lo = 0; }
+    else if (mat_type == 3) { hi = 27.0e+9; lo = 0; }
+    for (int iz = z1; iz < dimz; iz += fwi_dz)
+        for (int ix = x1; ix < dimx; ix += fwi_dx) {
+            double mv = IX2(mat, iz, ix, pitch), gv = IX2(grad, iz, ix, gpitch);
+            if (mv > mat_max) mat_max = mv;
+            /* the reference stores the signed value of the largest |grad| */
+            if (fabs(gv) > grad_max) grad_max = gv;
+        }
+    double sn = step_length * (mat_max / grad_max);
+    for (int iz = z1; iz < dimz; iz += fwi_dz)
+        for (int ix = x1; ix < dimx; ix += fwi_dx) {
+            double* nv = &IX2(mat_new, iz, ix, pitch);
+            *nv = IX2(mat, iz, ix, pitch) + sn * IX2(grad, iz, ix, gpitch);
+            if (*nv < lo) *nv = lo;
+            if (*nv > hi) *nv = hi;
+            if (*nv < 0.0) *nv = IX2(mat, iz, ix, pitch);
+        }
+    if (override_)
+        for (int iz = z1; iz < dimz; iz += fwi_dz)
+            for (int ix = x1; ix < dimx; ix += fwi_dx)
+                IX2(mat, iz, ix, pitch) = IX2(mat_new, iz, ix, pitch);
+}
+
+double orc_calc_opt_step(const double* L2, const double* sl) {
+    /* Gauss elimination with the reference's float multiplier and float
+     * back-substitution accumulator (solvelin.cu:10).  The reference starts its
+     * back substitution one row past the end (solvelin.cu:29), which reads
+     * outside the arrays; this restatement starts at the last row. */
+    double A[3][3], b[3], x[3] = {0, 0, 0};
+    for (int i = 0; i < 3; i++) { A[i][2] = sl[i] * sl[i]; A[i][1] = sl[i]; A[i][0] = 1.0; b[i] = L2[i]; }
+    for (int k = 0; k < 2; k++)
+        for (int n = k; n < 2; n++) {
+            float a = (float)(A[n + 1][k] / A[k][k]);
+            for (int mm = 0; mm < 3; mm++) A[n + 1][mm] = A[n + 1][mm] - a * A[k][mm];
+            b[n + 1] = b[n + 1] - a * b[k];
+        }
+    for (int k = 2; k >= 0; k--) {
+        float c = (float)b[k];
+        for (int mm = 2; mm > k; mm--) c = (float)(c - A[k][mm] * x[mm]);
+        x[k] = c / A[k][k];
+    }
+    return -x[1] / (2.0 * x[2]);
+}

@@ -1,0 +1,134 @@
+"""C ABI library on the CPU: it loads, exports every declared symbol, its
+host-side setup matches the oracle bit for bit, the checkpoint planner is
+valid and optimal, and errors come back as status codes (no GPU needed)."""
+import ctypes as C
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from cuda_fwi_gb300 import _capi
+from cuda_fwi_gb300 import problem as P
+from oracle import oracle as O
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+def declared_c_symbols():
+    text = (ROOT / "include" / "fwi_psv.h").read_text()
+    return sorted(set(re.findall(r"\b(fwi_psv_\w+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_symbol():
+    L = _capi.lib()
+    declared = declared_c_symbols()
+    assert len(declared) >= 25
+    for name in declared:
+        assert hasattr(L, name), name
+    # the ctypes table covers the whole header
+    assert set(declared) == set(_capi.exported_symbols())
+
+
+def test_cpp_reference_shims_exported():
+    import subprocess
+    out = subprocess.run(["nm", "-D", "-C", str(_capi.LIB_PATH)], capture_output=True, text=True).stdout
+    assert "forward_kernel_PSV_GPU(int, int, int, int, int, int, double" in out
+    assert "adjoint_kernel_PSV_GPU(int, int, int, int, int, int, double" in out
+
+
+def test_abi_version_and_strerror():
+    L = _capi.lib()
+    assert L.fwi_psv_abi_version() == 1
+    assert L.fwi_psv_strerror(0) == b"ok"
+    assert L.fwi_psv_strerror(-3) == b"out of memory"
+
+
+@pytest.mark.parametrize("order", [2, 4, 6, 8, 10, 12])
+def test_holberg_matches_oracle(order):
+    for err in range(5):
+        assert np.array_equal(_capi.holberg(order, err), O.holberg(order, err))
+
+
+def test_holberg_rejects_bad_order():
+    with pytest.raises(_capi.FwiError) as e:
+        _capi.holberg(7, 1)
+    assert e.value.code == "FWI_ERR_INVALID"
+
+
+@pytest.mark.parametrize("args", [(20, 10.0, 10.0, 2.0, 1.0, 1e-3, 3000.0, 1e-3),
+                                  (30, 5.0, 15.0, 2.0, 1.0, 1e-3, 4500.0, 0.5e-3),
+                                  (40, 7.5, 8.0, 3.0, 1.5, 1e-4, 5500.0, 0.6e-3)])
+def test_cpml_profile_matches_oracle(args):
+    a, b = _capi.cpml_profile(*args), O.cpml(*args)
+    for k in a:
+        assert np.array_equal(a[k], b[k]), k
+
+
+def test_average_wavelet_grid_match_oracle():
+    p = P.small(fdorder=4, perturb=0.1)
+    rho = p.rho.copy()
+    rho[2:5, 3:7] = 0.0
+    for x, y in zip(_capi.average_parameters(p.mu, rho), O.average(p.lam, p.mu, rho)):
+        assert np.array_equal(x, y)
+    assert np.array_equal(_capi.wavelet(400, 1e-3, 3.0, 11.0, 0.02), O.wavelet(400, 1e-3, 3.0, 11.0, 0.02))
+    for fs in (0, 1):
+        assert _capi.total_grid(200, 150, 8, 30, fs) == O.total_grid(200, 150, 8, 30, fs)
+
+
+def test_engine_reports_missing_device_or_bad_desc():
+    L = _capi.lib()
+    d = _capi.Desc()
+    h = C.c_void_p()
+    st = L.fwi_psv_create(C.byref(d), 0, C.byref(h))
+    assert st in (-8, -1, -2)  # no device here, or invalid descriptor on a GPU host
+    assert not h.value
+
+
+# ---- binomial checkpoint planner ------------------------------------------
+
+def simulate(plan, n, slots):
+    """Execute a plan abstractly; return the adjoint order and advance count."""
+    working, store, adj, adv = 0, {}, [], 0
+    for kind, a, b in plan:
+        if kind == 0:
+            assert working == a and b > a
+            adv += b - a
+            working = b
+        elif kind == 1:
+            assert working == b and 0 <= a < slots
+            store[a] = b
+        elif kind == 2:
+            assert (a == -1 and b == 0) or store.get(a) == b
+            working = b
+        else:
+            assert working == a, (working, a)
+            adj.append(a)
+    return adj, adv
+
+
+def dp_cost(n, s, memo={}):
+    if n <= 1:
+        return 0
+    if s == 0:
+        return n * (n - 1) // 2
+    key = (n, s)
+    if key not in memo:
+        memo[key] = min(j + dp_cost(n - j, s - 1) + dp_cost(j, s) for j in range(1, n))
+    return memo[key]
+
+
+@pytest.mark.parametrize("n,s", [(1, 0), (2, 1), (7, 0), (10, 2), (33, 3), (64, 4), (120, 5), (57, 1)])
+def test_checkpoint_plan_valid_and_optimal(n, s):
+    plan, cost = _capi.checkpoint_plan(n, s)
+    adj, adv = simulate(plan, n, s)
+    assert adj == list(range(n - 1, -1, -1))
+    assert adv == cost == dp_cost(n, s)
+
+
+def test_checkpoint_plan_large():
+    plan, cost = _capi.checkpoint_plan(3000, 32)
+    adj, adv = simulate(plan, 3000, 32)
+    assert adj == list(range(2999, -1, -1))
+    # Griewank-Walther bound with S = 33 stored states: r*n - beta(S+1, r-1), r = 3
+    assert cost == 3 * 3000 - 595 - 35
