@@ -1,0 +1,370 @@
+#!/usr/bin/env python
+"""Benchmark: batched, checkpointed shot-gradients/s on one GB300.
+
+Workload (the batched multi-shot gradient configuration): 1000x500 grid
+(1068x568 padded), dx=dz=10 m, dt=1 ms, nt=3000, 8th-order Holberg, 30-cell
+CPML, layered model with a dipping fault (observed data) and without it
+(synthetics), 64 shots x 250 receivers, binomial checkpointing with 32 slots
+per shot, gradients summed over shots.  One step = one batch of 64 shot
+gradients: forward sweep, residual, recompute + adjoint + gradient.
+
+Printed JSON line (rank 0):
+  value        shot-gradients/s, device-timed (CUDA events on the engine's
+               stream) with the observed data resident in HBM
+  e2e          the same through the public API with host buffers: the
+               observed data goes host->device and the summed gradient
+               device->host inside the timed region
+  roofline     the dominant kernel (forward stress pass) timed live with CUDA
+               events, algorithmic bytes per launch / duration vs measured HBM peak
+  cpu_baseline the FP64 CPU restatement of the reference path on the host cores
+  plain        the same gradient as one-shot-per-launch, no CUDA graph
+
+--impl reference times the CPU reference path (the oracle port of the
+reference's CPU forward/adjoint; the reference's own code implements only
+fdorder 2) on all host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+HBM_FALLBACK_GBS = 6800.0
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--shots", type=int, default=64)
+    ap.add_argument("--snapshots", type=int, default=32)
+    ap.add_argument("--nt", type=int, default=0, help="override nt (testing only)")
+    ap.add_argument("--plain-shots", type=int, default=1)
+    ap.add_argument("--cpu-nt-sample", type=int, default=24)
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return HBM_FALLBACK_GBS, "fallback"
+
+
+def workload(args):
+    from cuda_fwi_gb300 import problem as P
+    true = P.config3(True, nshots=args.shots)
+    syn = P.config3(False, nshots=args.shots)
+    if args.nt:
+        from dataclasses import replace
+        for name in ("true", "syn"):
+            p = locals()[name]
+            q = replace(p, nt=args.nt, src_signal=p.src_signal[:, : args.nt].copy())
+            if name == "true":
+                true = q
+            else:
+                syn = q
+    return true, syn
+
+
+WORKLOAD_DESC = ("1000x500 (1068x568 padded) elastic P-SV, dx=dz=10 m, dt=1 ms, nt=3000, "
+                 "8th-order Holberg, 30-cell CPML, faulted layered model, 64 shots x 250 receivers, "
+                 "binomial checkpointing 32 slots/shot, gradients summed over shots")
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if r[5 + i].lower() == "active"})
+        pw = [float(r[3]) for r in self.rows if r[3].replace(".", "").isdigit()]
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows),
+                "power_w_median": statistics.median(pw) if pw else None}
+
+
+def cpu_baseline(syn, args, nproc=None):
+    from oracle import cpu_bench
+    r = cpu_bench.time_gradient_sample(syn, nt_sample=args.cpu_nt_sample, nproc=nproc)
+    return {"value": r["shot_gradients_per_s"], "unit": "shot-gradients/s", "cores": r["cores"],
+            "kind": "port",
+            "sample": (f"{r['cores']} concurrent single-thread processes, each one shot-gradient "
+                       f"(forward with full storage + adjoint + gradient, FP64 order-8 restatement of the "
+                       f"reference CPU path) over {r['nt_sample']} of {syn.nt} time steps on the full "
+                       f"1068x568 grid, time scaled by nt/{r['nt_sample']}; {r['sample_s']:.1f} s wall"),
+            "gcell_upd_s": r["gcell_per_s"]}
+
+
+def run_reference(args, rank):
+    if rank != 0:
+        return
+    t0 = time.perf_counter()
+    _, syn = workload(args)
+    vals = []
+    last = None
+    for i in range(args.warmup + args.steps):
+        last = cpu_baseline(syn, args)
+        if i >= args.warmup:
+            vals.append(last["value"])
+    v = statistics.mean(vals)
+    last["value"] = v
+    out = {"impl": "reference", "metric": "shot-gradients/s", "value": v, "unit": "shot-gradients/s",
+           "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "data": "synthetic", "config": {"workload": WORKLOAD_DESC},
+           "cpu_baseline": last,
+           "e2e": {"value": v, "unit": "shot-gradients/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+           "wall_s": time.perf_counter() - t0}
+    print(json.dumps(out), flush=True)
+
+
+def algorithmic_bytes(p, B):
+    """Minimal DRAM bytes of one launch over B shots (FP32): per-shot fields
+    once, shared materials once per launch, CPML memory of strip cells."""
+    fp = p.fpad
+    nxi, nzi = p.nxt - 2 * fp, p.nzt - 2 * fp
+    cells = nxi * nzi
+    cpml_cells = 2 * p.npml * nzi + 2 * p.npml * nxi
+    stress_fwd = B * (cells * (8 + 24) + cpml_cells * 16) + cells * 12
+    vel_fwd = B * (cells * (12 + 16) + cpml_cells * 16) + cells * 8  # recompute sweeps: no energy
+    # adjoint: + ux,uz r/w (16) + 5 forward fields (20) + 3 gradients r/w (24) at a sampled step
+    stress_adj = B * (cells * (8 + 24 + 16 + 20 + 24) + cpml_cells * 16) + cells * 12
+    vel_adj = B * (cells * (12 + 16 + 8) + cpml_cells * 16) + cells * 8
+    return stress_fwd, vel_fwd, stress_adj, vel_adj
+
+
+def main():
+    args = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        return run_reference(args, rank)
+
+    true, syn = workload(args)
+    # CPU baseline first: its spawn pool starts before any CUDA call.
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        try:
+            cpu = cpu_baseline(syn, args)
+        except Exception as e:  # reported, never silently replaced
+            cpu = {"value": None, "error": repr(e)}
+
+    import numpy as np
+    import torch
+    from cuda_fwi_gb300.engine import Engine
+
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    shots = list(range(args.shots))
+    with Engine(true, device=local) as e:
+        e.set_exec(use_graphs=True)
+        obs, _ = e.forward(shots)
+    obs = np.ascontiguousarray(obs)
+
+    stream = torch.cuda.Stream(device=local)
+    eng = Engine(syn, device=local)
+    eng.set_stream(stream.cuda_stream)
+    eng.set_strategy("binomial", snapshots=args.snapshots)
+    gbuf = torch.zeros(3, syn.nfz, syn.nfx, dtype=torch.float64)
+
+    def step_resident():
+        eng.forward(shots, None, keep=True, want_rec=False, resident=True)
+        eng.backward(sum_shots=True, want=False)
+
+    def step_e2e():
+        _, mis = eng.forward(shots, obs, keep=True, want_rec=False)
+        g = eng.backward(sum_shots=True)
+        if dist is not None:
+            t = torch.from_numpy(np.stack(g)).cuda(local)
+            dist.all_reduce(t)
+            t.cpu()
+        return mis
+
+    # warm-up (captures the CUDA graphs; first call uploads the observed data)
+    eng.forward(shots, obs, keep=True, want_rec=False)
+    eng.backward(sum_shots=True)
+    for _ in range(args.warmup):
+        step_resident()
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    # ---- device-timed region (observed data resident) ----
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        barrier()
+        ev0.record(stream)
+        launches = 0
+        for _ in range(args.steps):
+            step_resident()
+            launches += eng.stats()["launches"]
+        ev1.record(stream)
+        barrier()
+    dev_s = ev0.elapsed_time(ev1) / 1e3
+    st = eng.stats()
+    launches_per_step = launches / args.steps
+
+    # ---- end to end through the public API with host buffers ----
+    barrier()
+    t0 = time.perf_counter()
+    h2d = d2h = 0
+    for _ in range(args.steps):
+        step_e2e()
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    eng.forward(shots, obs, keep=True, want_rec=False)
+    h2d = eng.stats()["h2d_bytes"]
+    d2h = eng.stats()["d2h_bytes"]
+    eng.backward(sum_shots=True)
+    d2h += eng.stats()["d2h_bytes"]
+
+    def maxr(x):
+        if dist is None:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    dev_s, e2e_s = maxr(dev_s), maxr(e2e_s)
+    B = args.shots
+    cells = syn.nxt * syn.nzt
+    recompute = st["recompute_steps"]
+    steps_per_batch = syn.nt + recompute + syn.nt
+    value = world * B * args.steps / dev_s
+    gcell = world * B * cells * steps_per_batch * args.steps / dev_s / 1e9
+
+    # ---- roofline: live per-kernel timing on the batch ----
+    ms = eng.time_kernels(reps=20)
+    b_sf, b_vf, b_sa, b_va = algorithmic_bytes(syn, B)
+    counts = [syn.nt + recompute, syn.nt + recompute, syn.nt, syn.nt]
+    shares = [c * t for c, t in zip(counts, ms)]
+    names = ["stress_kernel<4,false> (forward/recompute stress+CPML)",
+             "velocity_kernel<4> (forward velocity+CPML+events)",
+             "stress_kernel<4,true> (adjoint stress+CPML+ux/uz+gradient)",
+             "velocity_kernel<4> (adjoint velocity+CPML+residual)"]
+    dom = max(range(4), key=lambda i: shares[i])
+    peak, peak_kind = peaks()
+    achieved = [b / (t / 1e3) / 1e9 for b, t in zip((b_sf, b_vf, b_sa, b_va), ms)]
+    traffic = None
+    tfile = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tfile):
+        try:
+            traffic = json.load(open(tfile)).get(names[dom].split(" ")[0] + f"@B{B}")
+        except Exception:
+            traffic = None
+
+    # ---- plain path: one shot per launch, no graph, same kernels/checkpointing ----
+    plain = None
+    if rank == 0 and args.plain_shots > 0:
+        pe = Engine(syn, device=local)
+        pe.set_exec(use_graphs=False)
+        pe.set_strategy("binomial", snapshots=args.snapshots)
+        pe.forward([0], obs, keep=True, want_rec=False)
+        pe.backward()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for s in range(args.plain_shots):
+            pe.forward([s], obs, keep=True, want_rec=False)
+            pe.backward()
+        torch.cuda.synchronize()
+        ps = (time.perf_counter() - t0) / args.plain_shots
+        plain = {"shot_gradients_s": 1.0 / ps, "batched_over_plain": (value / world) * ps,
+                 "how": f"{args.plain_shots} shot(s), one shot per launch, direct launches (no graph), "
+                        f"same kernels and binomial checkpointing; host wall clock"}
+        pe.close()
+
+    if rank == 0:
+        out = {
+            "metric": "shot-gradients/s", "value": value, "unit": "shot-gradients/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": dev_s / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD_DESC, "shots_per_step": B, "nt": syn.nt,
+                       "padded_grid": [syn.nzt, syn.nxt], "fdorder": syn.fdorder,
+                       "checkpoints_per_shot": args.snapshots,
+                       "l2": "inputs larger than L2 (per-step working set ~30 GB: 64 shot states, "
+                             "checkpoints, 192 MB observed data)",
+                       "parallelism": f"replicas x{world}, shots batched in one launch per time step"},
+            "gcell_upd_s": gcell,
+            "time_steps_per_shot_gradient": steps_per_batch,
+            "e2e": {"value": world * B * args.steps / e2e_s, "unit": "shot-gradients/s",
+                    "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+            "gpu_launches": int(launches_per_step * args.steps),
+            "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": achieved[dom],
+                         "peak": peak, "unit": "GB/s", "frac": achieved[dom] / peak,
+                         "peak_source": peak_kind, "traffic": traffic,
+                         "launch_ms": ms[dom], "algorithmic_bytes_per_launch": [b_sf, b_vf, b_sa, b_va][dom],
+                         "all_kernels": {n.split(" ")[0] + ("_adj" if i >= 2 else "_fwd"):
+                                         {"ms": ms[i], "GBps": achieved[i], "count_per_step": counts[i]}
+                                         for i, n in enumerate(names)}},
+            "plain": plain,
+            "cpu_baseline": cpu,
+            "clocks": clk.summary(),
+        }
+        print(json.dumps(out), flush=True)
+    eng.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

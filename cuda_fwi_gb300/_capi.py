@@ -23,6 +23,7 @@ ERRORS = {
 }
 FWI_STORE_FULL, FWI_STORE_BINOMIAL, FWI_STORE_RANDOM = 0, 1, 2
 FWI_GRAD_REFERENCE, FWI_GRAD_EXACT = 0, 1
+FWI_FWD_KEEP, FWI_FWD_RESIDENT_OBS = 1, 2
 
 
 class FwiLibraryMissing(RuntimeError):
@@ -49,7 +50,8 @@ class Desc(C.Structure):
 class Stats(C.Structure):
     _fields_ = [(n, C.c_int64) for n in ("launches", "forward_steps", "recompute_steps",
                                           "adjoint_steps", "device_bytes", "snapshots")] + [
-        ("last_forward_ms", C.c_double), ("last_backward_ms", C.c_double)]
+        ("last_forward_ms", C.c_double), ("last_backward_ms", C.c_double),
+        ("h2d_bytes", C.c_int64), ("d2h_bytes", C.c_int64)]
 
 
 _lib = None
@@ -81,6 +83,7 @@ _SIGS = {
     "fwi_psv_energy": (C.c_int, [C.c_void_p, C.c_int, dp, dp]),
     "fwi_psv_wavefield": (C.c_int, [C.c_void_p, C.c_int, C.c_int, dp, dp, dp, dp, dp]),
     "fwi_psv_get_stats": (C.c_int, [C.c_void_p, C.POINTER(Stats)]),
+    "fwi_psv_time_kernels": (C.c_int, [C.c_void_p, C.c_int, dp]),
     "fwi_psv_forward_kernel": (C.c_int, [C.c_int] * 6 + [C.c_double] * 3 + [C.c_int, C.c_int, dp, C.c_int]
                                + [dp] * 6 + [dp] * 5 + [C.c_int] + [dp] * 6 + [dp] * 8
                                + [C.c_int, ip, ip, ip, dp, ip] + [C.c_int, ip, ip, ip, dp, ip]

@@ -37,7 +37,11 @@ def _run(cmd):
     return r.stdout + r.stderr
 
 
-def build(force: bool = False, verbose_ptxas: bool = False) -> Path:
+def build(force: bool = False, verbose_ptxas: bool = False, defines=(), out: Path | None = None) -> Path:
+    """Compile the library; `defines` (e.g. ["FWI_MIN_BLOCKS=4"]) and `out`
+    build a variant into another directory."""
+    if defines or out:
+        return _build_variant(list(defines), Path(out) if out else OUT_DIR / "variant.so")
     OBJ_DIR.mkdir(parents=True, exist_ok=True)
     deps = [CSRC / h for h in HEADERS] + [ROOT / "include" / "fwi_psv.h", Path(__file__)]
     newest_dep = max(p.stat().st_mtime for p in deps if p.exists())
@@ -55,11 +59,24 @@ def build(force: bool = False, verbose_ptxas: bool = False) -> Path:
             logs = list(ex.map(_run, jobs))
     if jobs or not LIB.exists():
         tmp = LIB.with_suffix(".so.tmp")
-        _run([nvcc(), "-shared", *ARCH, "-o", str(tmp), *map(str, objs), "-lcudart"])
+        _run([nvcc(), "-shared", *ARCH, "-o", str(tmp), *map(str, objs)])
         os.replace(tmp, LIB)
     if verbose_ptxas:
         print("\n".join(logs))
     return LIB
+
+
+def _build_variant(defines, out: Path) -> Path:
+    out.parent.mkdir(parents=True, exist_ok=True)
+    objdir = out.parent / (out.stem + "_obj")
+    objdir.mkdir(exist_ok=True)
+    dflags = [f"-D{d}" for d in defines]
+    jobs = [[nvcc(), "-c", *ARCH, *NVFLAGS, *dflags, str(CSRC / u), "-o", str(objdir / (u + ".o"))]
+            for u in UNITS]
+    with ThreadPoolExecutor(max_workers=len(jobs)) as ex:
+        list(ex.map(_run, jobs))
+    _run([nvcc(), "-shared", *ARCH, "-o", str(out), *[str(objdir / (u + ".o")) for u in UNITS]])
+    return out
 
 
 if __name__ == "__main__":

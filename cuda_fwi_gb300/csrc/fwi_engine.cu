@@ -91,40 +91,52 @@ __global__ void sum_shots_kernel(const float* __restrict__ in, float* __restrict
 // ---------------------------------------------------------------------------
 // kernel dispatch on the half order
 // ---------------------------------------------------------------------------
-using LaunchFn = void (*)(dim3, dim3, cudaStream_t, const ItemDesc*, const Tile*, int, unsigned);
+using LaunchFn = void (*)(dim3, dim3, cudaStream_t, const ItemDesc*, const Tile*, int, int, unsigned);
+using OccFn = int (*)(int block);
 
 template <int FP, bool ADJ>
 static void launch_stress(dim3 g, dim3 b, cudaStream_t s, const ItemDesc* items, const Tile* tiles,
-                          int it, unsigned flags) {
-    stress_kernel<FP, ADJ><<<g, b, 0, s>>>(items, tiles, it, flags);
+                          int ntiles, int it, unsigned flags) {
+    stress_kernel<FP, ADJ><<<g, b, 0, s>>>(items, tiles, ntiles, it, flags);
 }
 template <int FP>
 static void launch_velocity(dim3 g, dim3 b, cudaStream_t s, const ItemDesc* items,
-                            const Tile* tiles, int it, unsigned flags) {
-    velocity_kernel<FP><<<g, b, 0, s>>>(items, tiles, it, flags);
+                            const Tile* tiles, int ntiles, int it, unsigned flags) {
+    velocity_kernel<FP><<<g, b, 0, s>>>(items, tiles, ntiles, it, flags);
+}
+template <int FP, bool ADJ>
+static int occ_stress(int block) {
+    int n = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, stress_kernel<FP, ADJ>, block, 0);
+    return n;
+}
+template <int FP>
+static int occ_velocity(int block) {
+    int n = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, velocity_kernel<FP>, block, 0);
+    return n;
 }
 
-static LaunchFn stress_fn(int fp, bool adj) {
-    switch (fp) {
-        case 1: return adj ? launch_stress<1, true> : launch_stress<1, false>;
-        case 2: return adj ? launch_stress<2, true> : launch_stress<2, false>;
-        case 3: return adj ? launch_stress<3, true> : launch_stress<3, false>;
-        case 4: return adj ? launch_stress<4, true> : launch_stress<4, false>;
-        case 5: return adj ? launch_stress<5, true> : launch_stress<5, false>;
-        case 6: return adj ? launch_stress<6, true> : launch_stress<6, false>;
-    }
-    return nullptr;
+struct KernelSet {
+    LaunchFn stress_f, stress_a, velocity;
+    OccFn occ_f, occ_a, occ_v;
+};
+
+template <int FP>
+static KernelSet kernel_set() {
+    return {launch_stress<FP, false>, launch_stress<FP, true>, launch_velocity<FP>,
+            occ_stress<FP, false>, occ_stress<FP, true>, occ_velocity<FP>};
 }
-static LaunchFn velocity_fn(int fp) {
+
+static KernelSet kernels_for(int fp) {
     switch (fp) {
-        case 1: return launch_velocity<1>;
-        case 2: return launch_velocity<2>;
-        case 3: return launch_velocity<3>;
-        case 4: return launch_velocity<4>;
-        case 5: return launch_velocity<5>;
-        case 6: return launch_velocity<6>;
+        case 1: return kernel_set<1>();
+        case 2: return kernel_set<2>();
+        case 3: return kernel_set<3>();
+        case 4: return kernel_set<4>();
+        case 5: return kernel_set<5>();
+        default: return kernel_set<6>();
     }
-    return nullptr;
 }
 
 // ---------------------------------------------------------------------------
@@ -164,6 +176,35 @@ struct DBuf {
 
 static size_t round_up(size_t v, size_t m) { return (v + m - 1) / m * m; }
 
+// page-locked host staging buffer (fast, asynchronous copies)
+struct HBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    HBuf() = default;
+    HBuf(const HBuf&) = delete;
+    HBuf& operator=(const HBuf&) = delete;
+    ~HBuf() {
+        if (p) cudaFreeHost(p);
+    }
+    int ensure(size_t n) {
+        if (n <= bytes && p) return FWI_OK;
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        bytes = 0;
+        if (cudaMallocHost(&p, n) != cudaSuccess) {
+            cudaGetLastError();
+            p = nullptr;
+            return fail(FWI_ERR_NOMEM, "cudaMallocHost of " + std::to_string(n) + " bytes failed");
+        }
+        bytes = n;
+        return FWI_OK;
+    }
+    template <class T>
+    T* as() const {
+        return static_cast<T*>(p);
+    }
+};
+
 // ---------------------------------------------------------------------------
 // engine
 // ---------------------------------------------------------------------------
@@ -198,7 +239,11 @@ struct Engine {
     DBuf d_fwd, d_adj, d_ws, d_wr, d_ux, d_uz, d_grad, d_gsum, d_store, d_snap;
     DBuf d_evcol_f, d_ev_f, d_evcol_a, d_ev_a, d_rec, d_obs, d_resid, d_rowmis, d_blow;
     DBuf d_items_f, d_items_a, d_tiles;
+    HBuf h_stage, h_rec, h_grad;
+    bool obs_valid = false;
     int ntiles = 0, bx = 128, tz = 32;
+    KernelSet ks{};
+    int grid_sf = 1, grid_sa = 1, grid_v = 1, num_sms = 1;
     int slots = 0;  // checkpoint slots per shot (binomial)
     bool fwd_kept = false, have_resid = false, bwd_done = false, grad_on = true;
     std::vector<Action> plan;
@@ -268,6 +313,8 @@ struct Engine {
         FWI_TRY(bind());
         CUDA_TRY(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
         own_stream = true;
+        ks = kernels_for(fpad);
+        CUDA_TRY(cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, device));
         FWI_TRY(d_cpml.ensure(cpml_h.size() * sizeof(float) + 16));
         CUDA_TRY(cudaMemcpy(d_cpml.p, cpml_h.data(), cpml_h.size() * sizeof(float),
                             cudaMemcpyHostToDevice));
@@ -425,6 +472,7 @@ struct Engine {
         drop_graphs();
         fwd_kept = false;
         bwd_done = false;
+        obs_valid = false;
         if (budget > 0 && batch_bytes(nb, want_slots, keep ? strategy : -1) + fixed_bytes() > budget)
             return fail(FWI_ERR_NOMEM, "batch does not fit the memory budget");
         B = nb;
@@ -517,6 +565,10 @@ struct Engine {
         std::vector<Tile> t;
         plan_tiles(B, t);
         ntiles = (int)t.size();
+        // persistent grids: resident capacity, never more blocks than tiles
+        grid_sf = std::max(1, std::min(ntiles, num_sms * std::max(1, ks.occ_f(bx))));
+        grid_sa = std::max(1, std::min(ntiles, num_sms * std::max(1, ks.occ_a(bx))));
+        grid_v = std::max(1, std::min(ntiles, num_sms * std::max(1, ks.occ_v(bx))));
         FWI_TRY(d_tiles.ensure(t.size() * sizeof(Tile)));
         CUDA_TRY(cudaMemcpyAsync(d_tiles.p, t.data(), t.size() * sizeof(Tile), cudaMemcpyHostToDevice, stream));
         CUDA_TRY(cudaStreamSynchronize(stream));
@@ -582,10 +634,11 @@ struct Engine {
 
     // ---- launches ----------------------------------------------------------
     void step(bool adj, int it, unsigned sflags, unsigned vflags) {
-        const dim3 g(ntiles), b(bx);
+        const dim3 b(bx);
         const ItemDesc* items = adj ? d_items_a.as<ItemDesc>() : d_items_f.as<ItemDesc>();
-        stress_fn(fpad, adj)(g, b, stream, items, d_tiles.as<Tile>(), it, sflags);
-        velocity_fn(fpad)(g, b, stream, items, d_tiles.as<Tile>(), it, vflags);
+        const Tile* tl = d_tiles.as<Tile>();
+        (adj ? ks.stress_a : ks.stress_f)(dim3(adj ? grid_sa : grid_sf), b, stream, items, tl, ntiles, it, sflags);
+        ks.velocity(dim3(grid_v), b, stream, items, tl, ntiles, it, vflags);
         launches_now += 2;
     }
 
@@ -645,22 +698,28 @@ struct Engine {
     std::map<std::string, int64_t> graph_launches;
 
     // ---- forward -------------------------------------------------------------
-    int forward(int nb, const int* ids, const double* obs, double* rec_out, double* misfit, int keep) {
+    int forward(int nb, const int* ids, const double* obs_in, double* rec_out, double* misfit, int flags) {
         FWI_TRY(bind());
+        const int keep = flags & FWI_FWD_KEEP;
+        const bool resident = (flags & FWI_FWD_RESIDENT_OBS) != 0;
         FWI_TRY(setup_batch(nb, ids, keep != 0));
+        if (resident && !obs_valid)
+            return fail(FWI_ERR_STATE, "no observed data resident for this batch");
         const size_t nrows = rows.size();
+        const bool obs = resident || obs_in != nullptr;  // misfit + residual wanted
+        if (obs_in && !resident && nrows) {
+            FWI_TRY(h_stage.ensure(nrows * nt * 4));
+            float* o = h_stage.as<float>();
+            for (size_t k = 0; k < nrows; k++)
+                for (int t = 0; t < nt; t++) o[k * nt + t] = (float)obs_in[(size_t)rows[k] * nt + t];
+            CUDA_TRY(cudaMemcpyAsync(d_obs.p, o, nrows * nt * 4, cudaMemcpyHostToDevice, stream));
+            obs_valid = true;
+        }
         cudaEvent_t e0, e1;
         CUDA_TRY(cudaEventCreate(&e0));
         CUDA_TRY(cudaEventCreate(&e1));
         launches_now = 0;
         CUDA_TRY(cudaEventRecord(e0, stream));
-        if (obs && nrows) {
-            std::vector<float> o(nrows * nt);
-            for (size_t k = 0; k < nrows; k++)
-                for (int t = 0; t < nt; t++) o[k * nt + t] = (float)obs[(size_t)rows[k] * nt + t];
-            CUDA_TRY(cudaMemcpyAsync(d_obs.p, o.data(), o.size() * 4, cudaMemcpyHostToDevice, stream));
-            CUDA_TRY(cudaStreamSynchronize(stream));
-        }
         const bool store = keep && strategy == FWI_STORE_FULL;
         const bool ckpt = keep && strategy == FWI_STORE_BINOMIAL;
         // checkpoint positions of the first sweep: the SAVE actions before the first ADJOINT
@@ -672,6 +731,7 @@ struct Engine {
             }
         const std::string key = std::string("fwd") + (store ? "S" : "") + (ckpt ? "C" : "") +
                                 (obs ? "O" : "");
+        (void)obs_in;
         FWI_TRY(run_phase(key, [&]() -> int {
             CUDA_TRY(cudaMemsetAsync(d_fwd.p, 0, (size_t)B * state * 4, stream));
             CUDA_TRY(cudaMemsetAsync(d_ws.p, 0, (size_t)B * field * 4, stream));
@@ -693,11 +753,12 @@ struct Engine {
             return FWI_OK;
         }));
         CUDA_TRY(cudaEventRecord(e1, stream));
-        std::vector<float> rec(nrows * nt);
+        FWI_TRY(h_rec.ensure(rec_out ? nrows * nt * 4 : 16));
+        float* rec = h_rec.as<float>();
         std::vector<double> rm(nrows);
         int blow = 0;
         if (nrows && rec_out)
-            CUDA_TRY(cudaMemcpyAsync(rec.data(), d_rec.p, rec.size() * 4, cudaMemcpyDeviceToHost, stream));
+            CUDA_TRY(cudaMemcpyAsync(rec, d_rec.p, nrows * nt * 4, cudaMemcpyDeviceToHost, stream));
         if (nrows && obs) {
             CUDA_TRY(cudaMemcpyAsync(rm.data(), d_rowmis.p, nrows * 8, cudaMemcpyDeviceToHost, stream));
             CUDA_TRY(cudaMemcpyAsync(&blow, d_blow.p, 4, cudaMemcpyDeviceToHost, stream));
@@ -717,15 +778,56 @@ struct Engine {
         if (rec_out)
             for (size_t k = 0; k < nrows; k++)
                 for (int t = 0; t < nt; t++) rec_out[(size_t)rows[k] * nt + t] = (double)rec[k * nt + t];
+        stats.h2d_bytes = (obs_in && !resident) ? (int64_t)(nrows * nt * 4) : 0;
+        stats.d2h_bytes = (int64_t)((rec_out ? nrows * nt * 4 : 0) + (obs ? nrows * 8 + 4 : 0));
         if (misfit) {
             for (int b = 0; b < B; b++) misfit[b] = 0.0;
             if (obs)
                 for (size_t k = 0; k < nrows; k++) misfit[row_slot[k]] += rm[k];
         }
-        have_resid = obs != nullptr;
+        have_resid = obs;
         fwd_kept = keep != 0;
         bwd_done = false;
         if (blow) return fail(FWI_ERR_DIVERGED, "|syn - obs| exceeded 1e10 (the reference aborts here)");
+        return FWI_OK;
+    }
+
+    // Average device time of each hot kernel on the current batch.
+    int time_kernels(int reps, double ms[4]) {
+        FWI_TRY(bind());
+        if (B == 0) return fail(FWI_ERR_STATE, "run a forward first (it lays out the batch)");
+        if (reps < 1) return fail(FWI_ERR_INVALID, "reps must be >= 1");
+        cudaEvent_t a, b;
+        CUDA_TRY(cudaEventCreate(&a));
+        CUDA_TRY(cudaEventCreate(&b));
+        const dim3 blk(bx);
+        const Tile* tl = d_tiles.as<Tile>();
+        const ItemDesc* itf = d_items_f.as<ItemDesc>();
+        const ItemDesc* ita = d_items_a.as<ItemDesc>();
+        const bool have_adj_src = strategy != FWI_STORE_BINOMIAL ? d_store.p != nullptr : true;
+        for (int k = 0; k < 4; k++) {
+            const bool adj = k >= 2;
+            if (adj && !have_adj_src) { ms[k] = 0.0; continue; }
+            const int it = fwi_dt * (nft - 1);  // a sampled step: the gradient runs
+            auto launch = [&]() {
+                if (k == 0) ks.stress_f(dim3(grid_sf), blk, stream, itf, tl, ntiles, it, 0u);
+                if (k == 1) ks.velocity(dim3(grid_v), blk, stream, itf, tl, ntiles, it, FL_INJECT | FL_WE);
+                if (k == 2) ks.stress_a(dim3(grid_sa), blk, stream, ita, tl, ntiles, it, FL_GRAD);
+                if (k == 3) ks.velocity(dim3(grid_v), blk, stream, ita, tl, ntiles, it, FL_INJECT | FL_WE);
+            };
+            launch();  // warm-up
+            CUDA_TRY(cudaEventRecord(a, stream));
+            for (int r = 0; r < reps; r++) launch();
+            CUDA_TRY(cudaEventRecord(b, stream));
+            CUDA_TRY(cudaEventSynchronize(b));
+            float t = 0.f;
+            CUDA_TRY(cudaEventElapsedTime(&t, a, b));
+            ms[k] = t / reps;
+        }
+        CUDA_TRY(cudaGetLastError());
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+        fwd_kept = false;
         return FWI_OK;
     }
 
@@ -796,10 +898,15 @@ struct Engine {
         CUDA_TRY(cudaEventRecord(e1, stream));
         const bool summed = sum_shots && B > 1;
         const size_t ntrip = summed ? 1 : (size_t)B;
-        std::vector<float> g(ntrip * 3 * nf);
-        CUDA_TRY(cudaMemcpyAsync(g.data(), summed ? d_gsum.p : d_grad.p, g.size() * 4,
-                                 cudaMemcpyDeviceToHost, stream));
+        const bool want = gl || gm || gr;
+        FWI_TRY(h_grad.ensure(want ? ntrip * 3 * nf * 4 : 16));
+        const float* g = h_grad.as<float>();
+        if (want)
+            CUDA_TRY(cudaMemcpyAsync(h_grad.p, summed ? d_gsum.p : d_grad.p, ntrip * 3 * nf * 4,
+                                     cudaMemcpyDeviceToHost, stream));
         CUDA_TRY(cudaStreamSynchronize(stream));
+        stats.h2d_bytes = 0;
+        stats.d2h_bytes = want ? (int64_t)(ntrip * 3 * nf * 4) : 0;
         float ms = 0.f;
         cudaEventElapsedTime(&ms, e0, e1);
         cudaEventDestroy(e0);
@@ -810,9 +917,9 @@ struct Engine {
         stats.recompute_steps = strategy == FWI_STORE_BINOMIAL
                                     ? (recompute > 0 ? recompute : plan_cost) * fwi_dt
                                     : 0;
-        for (size_t s = 0; s < ntrip; s++)
+        for (size_t s = 0; s < ntrip && want; s++)
             for (size_t i = 0; i < nf; i++) {
-                const float* t = g.data() + s * 3 * nf;
+                const float* t = g + s * 3 * nf;
                 if (gl) gl[s * nf + i] = t[i];
                 if (gm) gm[s * nf + i] = t[nf + i];
                 if (gr) gr[s * nf + i] = t[2 * nf + i];
@@ -1120,9 +1227,9 @@ int fwi_psv_set_exec(fwi_psv_engine* h, int use_graphs, int block_x, int tile_z)
 }
 
 int fwi_psv_forward(fwi_psv_engine* h, int nshots, const int* shots, const double* obs,
-                    double* rec_out, double* misfit, int keep) {
+                    double* rec_out, double* misfit, int flags) {
     GUARD_ENGINE(h);
-    return h->e.forward(nshots, shots, obs, rec_out, misfit, keep);
+    return h->e.forward(nshots, shots, obs, rec_out, misfit, flags);
 }
 
 int fwi_psv_backward(fwi_psv_engine* h, double* gl, double* gm, double* gr, int sum_shots) {
@@ -1140,6 +1247,12 @@ int fwi_psv_wavefield(fwi_psv_engine* h, int which, int slot, double* vx, double
     GUARD_ENGINE(h);
     double* out[5] = {vx, vz, sxx, szx, szz};
     return h->e.wavefield(which, slot, out);
+}
+
+int fwi_psv_time_kernels(fwi_psv_engine* h, int reps, double ms[4]) {
+    GUARD_ENGINE(h);
+    if (!ms) return fail(FWI_ERR_INVALID, "null ms");
+    return h->e.time_kernels(reps, ms);
 }
 
 int fwi_psv_get_stats(fwi_psv_engine* h, fwi_psv_stats* out) {

@@ -95,23 +95,39 @@ class Engine:
         check(_capi.lib().fwi_psv_set_stream(self.h, C.c_void_p(stream_handle or 0)), "set_stream")
 
     # ---- forward / backward -------------------------------------------------
-    def forward(self, shots, obs=None, keep=False, want_rec=True):
+    def forward(self, shots, obs=None, keep=False, want_rec=True, resident=False):
+        """Run the shots together.  obs [nrec][nt] (host, FP64) or, with
+        resident=True, the observed data left on the device by the previous
+        forward of the same batch.  Returns (rec [nrec][nt] or None, misfit [nshots])."""
         shots = _i32(np.atleast_1d(shots))
         rec = np.zeros((max(self.nrec, 1), self.p.nt)) if want_rec else None
         mis = np.zeros(len(shots))
-        o = _f64(obs) if obs is not None else None
+        o = _f64(obs) if (obs is not None and not resident) else None
+        flags = (_capi.FWI_FWD_KEEP if keep else 0) | (_capi.FWI_FWD_RESIDENT_OBS if resident else 0)
         check(_capi.lib().fwi_psv_forward(self.h, len(shots), pi(shots), pd(o), pd(rec), pd(mis),
-                                          int(keep)), "forward")
+                                          flags), "forward")
         self._last_nshots = len(shots)
         return rec, mis
 
-    def backward(self, sum_shots=False):
+    def backward(self, sum_shots=False, want=True):
+        """Gradients (lam, mu, rho) [nshots][nfz][nfx], or summed over the
+        batch; want=False leaves them on the device (returns None)."""
+        if not want:
+            check(_capi.lib().fwi_psv_backward(self.h, None, None, None, int(sum_shots)), "backward")
+            return None
         n = 1 if sum_shots else self._last_nshots
         g = [np.zeros((n, self.nfz, self.nfx)) for _ in range(3)]
         check(_capi.lib().fwi_psv_backward(self.h, *[pd(x) for x in g], int(sum_shots)), "backward")
         if sum_shots:
             g = [x[0] for x in g]
         return tuple(g)
+
+    def time_kernels(self, reps=20):
+        """Average device ms of one launch of: forward stress, forward velocity,
+        adjoint stress, adjoint velocity (drops the retained forward)."""
+        ms = np.zeros(4)
+        check(_capi.lib().fwi_psv_time_kernels(self.h, reps, pd(ms)), "time_kernels")
+        return [float(x) for x in ms]
 
     def energy(self, slot=0):
         ws = np.zeros((self.p.nzt, self.p.nxt))

@@ -152,14 +152,18 @@ int fwi_psv_set_strategy(fwi_psv_engine* e, int strategy, int snapshots, size_t 
 int fwi_psv_set_gradient_mode(fwi_psv_engine* e, int mode);
 
 /* Forward pass for `nshots` shots (ids in `shots`) run together on the device.
- *   obs      [nrec][nt] observed data, or NULL (no misfit, no backward).
+ *   obs      [nrec][nt] observed data, or NULL (no misfit; backward then needs
+ *            a residual from elsewhere).
  *   rec_out  [nrec][nt] synthetic seismograms (rows of receivers recorded by
  *            a shot of this batch are written, others untouched), or NULL.
  *   misfit   [nshots] per-shot J = sum 0.5 dt (syn-obs)^2, or NULL.
- *   keep     non-zero: retain what backward needs (storage or checkpoints).
+ *   flags    FWI_FWD_KEEP: retain what backward needs (storage or checkpoints);
+ *            FWI_FWD_RESIDENT_OBS: reuse the observed data already on the device
+ *            from the previous forward of the same batch (obs is ignored).
  */
+enum { FWI_FWD_KEEP = 1, FWI_FWD_RESIDENT_OBS = 2 };
 int fwi_psv_forward(fwi_psv_engine* e, int nshots, const int* shots, const double* obs,
-                    double* rec_out, double* misfit, int keep);
+                    double* rec_out, double* misfit, int flags);
 
 /* Backward for the batch of the last forward(keep=1): adjoint pass driven by
  * the residual at the receivers, gradient accumulation.  Gradients are
@@ -182,7 +186,8 @@ int fwi_psv_wavefield(fwi_psv_engine* e, int which, int slot, double* vx, double
 typedef struct fwi_psv_stats {
     int64_t launches, forward_steps, recompute_steps, adjoint_steps;
     int64_t device_bytes, snapshots;
-    double last_forward_ms, last_backward_ms;
+    double last_forward_ms, last_backward_ms;  /* device time of the compute (CUDA events) */
+    int64_t h2d_bytes, d2h_bytes;              /* host<->device bytes of the last call */
 } fwi_psv_stats;
 int fwi_psv_get_stats(fwi_psv_engine* e, fwi_psv_stats* out);
 
@@ -195,6 +200,13 @@ int fwi_psv_get_stats(fwi_psv_engine* e, fwi_psv_stats* out);
  * cap is too small, with *count = actions needed); *forward_steps = advance cost. */
 int fwi_psv_checkpoint_plan(int nsteps, int slots, int* actions, int cap, int* count,
                             long long* forward_steps);
+
+/* Device time of one launch of each hot kernel on the current batch, averaged
+ * over `reps` launches timed with CUDA events on the engine's stream:
+ * ms[0] forward stress, ms[1] forward velocity (+energy, events), ms[2] adjoint
+ * stress (+ux/uz, gradient), ms[3] adjoint velocity.  Needs a prior forward;
+ * it overwrites the wavefield state (the retained forward is dropped). */
+int fwi_psv_time_kernels(fwi_psv_engine* e, int reps, double ms[4]);
 
 /* Execution options: use_graphs != 0 captures the time loop in CUDA graphs
  * (default 1); block_x / tile_z override the autotuned tile (0 = auto). */
