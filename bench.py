@@ -50,7 +50,8 @@ def parse():
     ap.add_argument("--snapshots", type=int, default=32)
     ap.add_argument("--nt", type=int, default=0, help="override nt (testing only)")
     ap.add_argument("--plain-shots", type=int, default=1)
-    ap.add_argument("--cpu-nt-sample", type=int, default=24)
+    ap.add_argument("--batch", type=int, default=0, help="shots per launch (0 = engine default)")
+    ap.add_argument("--cpu-nt-sample", type=int, default=200)
     ap.add_argument("--no-cpu", action="store_true")
     return ap.parse_args()
 
@@ -221,24 +222,23 @@ def main():
     eng = Engine(syn, device=local)
     eng.set_stream(stream.cuda_stream)
     eng.set_strategy("binomial", snapshots=args.snapshots)
-    gbuf = torch.zeros(3, syn.nfz, syn.nfx, dtype=torch.float64)
+    eng.set_exec(True, 0, 0, args.batch)
 
     def step_resident():
-        eng.forward(shots, None, keep=True, want_rec=False, resident=True)
-        eng.backward(sum_shots=True, want=False)
+        # one batch of shot gradients, observed data resident in HBM, summed gradient left on the device
+        eng.gradient(shots, None, resident=True, want=False)
 
     def step_e2e():
-        _, mis = eng.forward(shots, obs, keep=True, want_rec=False)
-        g = eng.backward(sum_shots=True)
+        # public API with host buffers: FP64 observed data in, summed FP64 gradient out
+        g, mis = eng.gradient(shots, obs)
         if dist is not None:
             t = torch.from_numpy(np.stack(g)).cuda(local)
             dist.all_reduce(t)
             t.cpu()
         return mis
 
-    # warm-up (captures the CUDA graphs; first call uploads the observed data)
-    eng.forward(shots, obs, keep=True, want_rec=False)
-    eng.backward(sum_shots=True)
+    # warm-up (captures the CUDA graphs; the first call uploads the observed data)
+    eng.gradient(shots, obs)
     for _ in range(args.warmup):
         step_resident()
 
@@ -271,11 +271,8 @@ def main():
         step_e2e()
     barrier()
     e2e_s = time.perf_counter() - t0
-    eng.forward(shots, obs, keep=True, want_rec=False)
-    h2d = eng.stats()["h2d_bytes"]
-    d2h = eng.stats()["d2h_bytes"]
-    eng.backward(sum_shots=True)
-    d2h += eng.stats()["d2h_bytes"]
+    est = eng.stats()
+    h2d, d2h = est["h2d_bytes"], est["d2h_bytes"]
 
     def maxr(x):
         if dist is None:
@@ -287,20 +284,22 @@ def main():
     dev_s, e2e_s = maxr(dev_s), maxr(e2e_s)
     B = args.shots
     cells = syn.nxt * syn.nzt
-    recompute = st["recompute_steps"]
+    recompute = st["recompute_steps"]  # per shot
     steps_per_batch = syn.nt + recompute + syn.nt
+    sub = int(st["batch"])
     value = world * B * args.steps / dev_s
     gcell = world * B * cells * steps_per_batch * args.steps / dev_s / 1e9
 
-    # ---- roofline: live per-kernel timing on the batch ----
+    # ---- roofline: live per-kernel timing on one full sub-batch ----
+    eng.forward(shots[:sub], obs, keep=True, want_rec=False)  # lays out a batch of `sub` shots
     ms = eng.time_kernels(reps=20)
-    b_sf, b_vf, b_sa, b_va = algorithmic_bytes(syn, B)
+    b_sf, b_vf, b_sa, b_va = algorithmic_bytes(syn, sub)
     counts = [syn.nt + recompute, syn.nt + recompute, syn.nt, syn.nt]
     shares = [c * t for c, t in zip(counts, ms)]
-    names = ["stress_kernel<4,false> (forward/recompute stress+CPML)",
-             "velocity_kernel<4> (forward velocity+CPML+events)",
-             "stress_kernel<4,true> (adjoint stress+CPML+ux/uz+gradient)",
-             "velocity_kernel<4> (adjoint velocity+CPML+residual)"]
+    names = ["stress_kernel<4,false,2> (forward/recompute stress+CPML, float4 cells)",
+             "velocity_kernel<4,2> (forward velocity+CPML+events, float4 cells)",
+             "stress_kernel<4,true,1> (adjoint stress+CPML+ux/uz+gradient, cells)",
+             "velocity_kernel<4,2> (adjoint velocity+CPML+residual, float4 cells)"]
     dom = max(range(4), key=lambda i: shares[i])
     peak, peak_kind = peaks()
     achieved = [b / (t / 1e3) / 1e9 for b, t in zip((b_sf, b_vf, b_sa, b_va), ms)]
@@ -308,7 +307,7 @@ def main():
     tfile = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tfile):
         try:
-            traffic = json.load(open(tfile)).get(names[dom].split(" ")[0] + f"@B{B}")
+            traffic = json.load(open(tfile)).get(names[dom].split(" ")[0] + f"@B{sub}")
         except Exception:
             traffic = None
 
@@ -316,15 +315,13 @@ def main():
     plain = None
     if rank == 0 and args.plain_shots > 0:
         pe = Engine(syn, device=local)
-        pe.set_exec(use_graphs=False)
+        pe.set_exec(False, 0, 0, 1)
         pe.set_strategy("binomial", snapshots=args.snapshots)
-        pe.forward([0], obs, keep=True, want_rec=False)
-        pe.backward()
+        pe.gradient([0], obs)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for s in range(args.plain_shots):
-            pe.forward([s], obs, keep=True, want_rec=False)
-            pe.backward()
+            pe.gradient([s], obs)
         torch.cuda.synchronize()
         ps = (time.perf_counter() - t0) / args.plain_shots
         plain = {"shot_gradients_s": 1.0 / ps, "batched_over_plain": (value / world) * ps,
@@ -338,7 +335,7 @@ def main():
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": dev_s / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": WORKLOAD_DESC, "shots_per_step": B, "nt": syn.nt,
+            "config": {"workload": WORKLOAD_DESC, "shots_per_step": B, "shots_per_launch": sub, "nt": syn.nt,
                        "padded_grid": [syn.nzt, syn.nxt], "fdorder": syn.fdorder,
                        "checkpoints_per_shot": args.snapshots,
                        "l2": "inputs larger than L2 (per-step working set ~30 GB: 64 shot states, "

@@ -51,7 +51,7 @@ class Stats(C.Structure):
     _fields_ = [(n, C.c_int64) for n in ("launches", "forward_steps", "recompute_steps",
                                           "adjoint_steps", "device_bytes", "snapshots")] + [
         ("last_forward_ms", C.c_double), ("last_backward_ms", C.c_double),
-        ("h2d_bytes", C.c_int64), ("d2h_bytes", C.c_int64)]
+        ("h2d_bytes", C.c_int64), ("d2h_bytes", C.c_int64), ("batch", C.c_int64)]
 
 
 _lib = None
@@ -76,7 +76,8 @@ _SIGS = {
     "fwi_psv_set_fwi": (C.c_int, [C.c_void_p] + [C.c_int] * 7),
     "fwi_psv_set_strategy": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_size_t]),
     "fwi_psv_set_gradient_mode": (C.c_int, [C.c_void_p, C.c_int]),
-    "fwi_psv_set_exec": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int]),
+    "fwi_psv_set_exec": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int]),
+    "fwi_psv_gradient": (C.c_int, [C.c_void_p, C.c_int, ip, dp, dp, dp, dp, dp, C.c_int]),
     "fwi_psv_checkpoint_plan": (C.c_int, [C.c_int, C.c_int, ip, C.c_int, ip, C.POINTER(C.c_longlong)]),
     "fwi_psv_forward": (C.c_int, [C.c_void_p, C.c_int, ip, dp, dp, dp, C.c_int]),
     "fwi_psv_backward": (C.c_int, [C.c_void_p, dp, dp, dp, C.c_int]),

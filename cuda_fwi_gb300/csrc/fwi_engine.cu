@@ -49,14 +49,16 @@ namespace fwi {
 // residual = syn - obs (in place into resid), per-row partial misfit sums in FP64
 // (fd_wave_model.cu:972-1002).  One block per receiver row.
 __global__ void residual_kernel(const float* __restrict__ syn, const float* __restrict__ obs,
-                                float* __restrict__ resid, double* __restrict__ row_misfit,
-                                int* __restrict__ blowup, int nt, double half_dt) {
+                                const int* __restrict__ row_rec, float* __restrict__ resid,
+                                double* __restrict__ row_misfit, int* __restrict__ blowup, int nt,
+                                double half_dt) {
     const int r = blockIdx.x;
     const size_t o = (size_t)r * nt;
+    const float* ob = obs + (size_t)row_rec[r] * nt;
     double acc = 0.0;
     int big = 0;
     for (int t = threadIdx.x; t < nt; t += blockDim.x) {
-        const double diff = (double)syn[o + t] - (double)obs[o + t];
+        const double diff = (double)syn[o + t] - (double)ob[t];
         acc += half_dt * diff * diff;
         resid[o + t] = (float)diff;
         big |= fabs(diff) > 1.0e10;
@@ -79,64 +81,80 @@ __global__ void residual_kernel(const float* __restrict__ syn, const float* __re
 
 // sum the per-shot gradient triples: out[i] = sum_b in[b*n + i]
 __global__ void sum_shots_kernel(const float* __restrict__ in, float* __restrict__ out, size_t n,
-                                 int nb) {
+                                 int nb, int accumulate) {
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
          i += (size_t)gridDim.x * blockDim.x) {
         float s = 0.f;
         for (int b = 0; b < nb; b++) s += in[(size_t)b * n + i];
-        out[i] = s;
+        out[i] = accumulate ? out[i] + s : s;
     }
 }
 
 // ---------------------------------------------------------------------------
 // kernel dispatch on the half order
 // ---------------------------------------------------------------------------
-using LaunchFn = void (*)(dim3, dim3, cudaStream_t, const ItemDesc*, const Tile*, int, int, unsigned);
-using OccFn = int (*)(int block);
+using LaunchFn = void (*)(dim3, cudaStream_t, const ItemDesc*, const Tile*, int, int, unsigned, int*);
+using OccFn = int (*)();
 
-template <int FP, bool ADJ>
-static void launch_stress(dim3 g, dim3 b, cudaStream_t s, const ItemDesc* items, const Tile* tiles,
-                          int ntiles, int it, unsigned flags) {
-    stress_kernel<FP, ADJ><<<g, b, 0, s>>>(items, tiles, ntiles, it, flags);
+template <int FP, bool ADJ, int MAP>
+static void launch_stress(dim3 g, cudaStream_t s, const ItemDesc* items, const Tile* tiles,
+                          int ntiles, int it, unsigned flags, int* err) {
+    stress_kernel<FP, ADJ, MAP><<<g, dim3(MapDims<MAP>::x, MapDims<MAP>::y), 0, s>>>(items, tiles, ntiles,
+                                                                                    it, flags, err);
 }
-template <int FP>
-static void launch_velocity(dim3 g, dim3 b, cudaStream_t s, const ItemDesc* items,
-                            const Tile* tiles, int ntiles, int it, unsigned flags) {
-    velocity_kernel<FP><<<g, b, 0, s>>>(items, tiles, ntiles, it, flags);
+template <int FP, int MAP>
+static void launch_velocity(dim3 g, cudaStream_t s, const ItemDesc* items, const Tile* tiles,
+                            int ntiles, int it, unsigned flags, int* err) {
+    velocity_kernel<FP, MAP><<<g, dim3(MapDims<MAP>::x, MapDims<MAP>::y), 0, s>>>(items, tiles, ntiles, it,
+                                                                                 flags, err);
 }
-template <int FP, bool ADJ>
-static int occ_stress(int block) {
+template <int FP, bool ADJ, int MAP>
+static int occ_stress() {
     int n = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, stress_kernel<FP, ADJ>, block, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, stress_kernel<FP, ADJ, MAP>,
+                                                  MapDims<MAP>::x * MapDims<MAP>::y, 0);
     return n;
 }
-template <int FP>
-static int occ_velocity(int block) {
+template <int FP, int MAP>
+static int occ_velocity() {
     int n = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, velocity_kernel<FP>, block, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, velocity_kernel<FP, MAP>,
+                                                  MapDims<MAP>::x * MapDims<MAP>::y, 0);
     return n;
 }
 
+// The kernels of one thread mapping: MAP 0 = z-march, 1 = cell-parallel.
 struct KernelSet {
     LaunchFn stress_f, stress_a, velocity;
     OccFn occ_f, occ_a, occ_v;
+    int map;
 };
 
-template <int FP>
+// The vectorised mapping (MAP 2) keeps the adjoint stress pass on the scalar
+// cell mapping: its per-cell gradient update does not vectorise and the
+// register-light scalar kernel runs it faster (measured: 43 us vs 76 us for
+// 2 shots of the 1068x568 grid, order 8).
+template <int FP, int MAP>
 static KernelSet kernel_set() {
-    return {launch_stress<FP, false>, launch_stress<FP, true>, launch_velocity<FP>,
-            occ_stress<FP, false>, occ_stress<FP, true>, occ_velocity<FP>};
+    constexpr int AMAP = MAP == 2 ? 1 : MAP;
+    return {launch_stress<FP, false, MAP>, launch_stress<FP, true, AMAP>, launch_velocity<FP, MAP>,
+            occ_stress<FP, false, MAP>, occ_stress<FP, true, AMAP>, occ_velocity<FP, MAP>, MAP};
 }
 
-static KernelSet kernels_for(int fp) {
+template <int MAP>
+static KernelSet kernels_for_map(int fp) {
     switch (fp) {
-        case 1: return kernel_set<1>();
-        case 2: return kernel_set<2>();
-        case 3: return kernel_set<3>();
-        case 4: return kernel_set<4>();
-        case 5: return kernel_set<5>();
-        default: return kernel_set<6>();
+        case 1: return kernel_set<1, MAP>();
+        case 2: return kernel_set<2, MAP>();
+        case 3: return kernel_set<3, MAP>();
+        case 4: return kernel_set<4, MAP>();
+        case 5: return kernel_set<5, MAP>();
+        default: return kernel_set<6, MAP>();
     }
+}
+static KernelSet kernels_for(int fp, int map) {
+    if (map == 2 && fp <= 4) return kernels_for_map<2>(fp);
+    return map ? kernels_for_map<1>(fp) : kernels_for_map<0>(fp);
 }
 
 // ---------------------------------------------------------------------------
@@ -237,12 +255,14 @@ struct Engine {
     std::vector<int> rows;  // receiver index of each batch row
     std::vector<int> row_slot;
     DBuf d_fwd, d_adj, d_ws, d_wr, d_ux, d_uz, d_grad, d_gsum, d_store, d_snap;
-    DBuf d_evcol_f, d_ev_f, d_evcol_a, d_ev_a, d_rec, d_obs, d_resid, d_rowmis, d_blow;
-    DBuf d_items_f, d_items_a, d_tiles;
+    DBuf d_evcol_f, d_ev_f, d_evcol_a, d_ev_a, d_rec, d_resid, d_rowmis, d_blow;
+    DBuf d_items_f, d_items_a;
     HBuf h_stage, h_rec, h_grad;
+    DBuf d_err;  // kernel error flags (bounded waits that timed out)
     bool obs_valid = false;
     int ntiles = 0, bx = 128, tz = 32;
     KernelSet ks{};
+    int kmap = 2;  // thread mapping of the stencil kernels (0 z-march, 1 cells, 2 vector cells)
     int grid_sf = 1, grid_sa = 1, grid_v = 1, num_sms = 1;
     int slots = 0;  // checkpoint slots per shot (binomial)
     bool fwd_kept = false, have_resid = false, bwd_done = false, grad_on = true;
@@ -313,8 +333,10 @@ struct Engine {
         FWI_TRY(bind());
         CUDA_TRY(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
         own_stream = true;
-        ks = kernels_for(fpad);
+        ks = kernels_for(fpad, kmap);
         CUDA_TRY(cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, device));
+        FWI_TRY(d_err.ensure(16));
+        CUDA_TRY(cudaMemset(d_err.p, 0, 16));
         FWI_TRY(d_cpml.ensure(cpml_h.size() * sizeof(float) + 16));
         CUDA_TRY(cudaMemcpy(d_cpml.p, cpml_h.data(), cpml_h.size() * sizeof(float),
                             cudaMemcpyHostToDevice));
@@ -330,6 +352,7 @@ struct Engine {
 
     void invalidate_batch() {
         drop_graphs();
+        for (auto& kv : tilesets) kv.second->ntiles = 0;
         B = 0;
         fwd_kept = false;
         bwd_done = false;
@@ -391,6 +414,7 @@ struct Engine {
                 return fail(FWI_ERR_INVALID, "receiver " + std::to_string(i) + " outside the interior");
         nrec = n;
         rx.assign(x, x + n); rz.assign(z, z + n); rcomp.assign(comp, comp + n); rshot.assign(shot, shot + n);
+        obs_valid = false;
         invalidate_batch();
         return FWI_OK;
     }
@@ -412,16 +436,18 @@ struct Engine {
     // ---- tiles -----------------------------------------------------------
     void plan_tiles(int nb, std::vector<Tile>& t) {
         const int nz_int = nzt - 2 * fpad;
-        bx = bx_req > 0 ? bx_req : (nxt >= 512 ? 128 : 64);
+        bx = kTileX;  // tile columns = threads per block
         const int ntx = (nxt + bx - 1) / bx;
-        if (tz_req > 0) {
+        if (ks.map == 1 || ks.map == 2) {
+            tz = ks.map == 1 ? MapDims<1>::rows : MapDims<2>::rows;  // one tile = one block's cells
+        } else if (tz_req > 0) {
             tz = tz_req;
         } else {
-            // enough blocks for >= 8 resident blocks per SM on 152 SMs, rows >= 4
-            const long long want = 8LL * 152;
-            long long per_shot = std::max<long long>(1, want / std::max(1, nb));
-            long long ntz = std::max<long long>(1, per_shot / ntx);
-            tz = (int)std::max<long long>(4, std::min<long long>(64, (nz_int + ntz - 1) / ntz));
+            // about four tiles per resident block (load balance), rows >= 8
+            const long long resident = (long long)num_sms * std::max(1, ks.occ_f());
+            const long long per_shot = std::max<long long>(1, 4 * resident / std::max(1, nb));
+            const long long ntz = std::max<long long>(1, per_shot / ntx);
+            tz = (int)std::max<long long>(8, std::min<long long>(128, (nz_int + ntz - 1) / ntz));
         }
         t.clear();
         for (int x0 = 0; x0 < nxt; x0 += bx)
@@ -430,82 +456,138 @@ struct Engine {
     }
 
     // ---- batch setup --------------------------------------------------------
+    // Buffers are sized for the largest batch seen (Bcap) and never shrink, so
+    // the device pointers captured in CUDA graphs stay valid for every smaller
+    // batch; a graph is keyed by the batch shape (B, receiver rows, slots,
+    // strategy), never by shot ids.  A reallocation drops all graphs.
     size_t batch_bytes(int nb, int nslots, int strat) const {
         size_t f = 4;
         size_t b = 0;
         b += 2 * (size_t)nb * state * f;        // fwd + adj state
         b += 4 * (size_t)nb * field * f;        // ws, wr, ux, uz
-        b += 3 * (size_t)nb * nf * f * 2;       // grads (+ sum)
+        b += 3 * (size_t)nb * nf * f + 6 * nf * f;  // grads, sum, accumulator
         if (strat == FWI_STORE_FULL) b += (size_t)nb * nft * 5 * nf * f;
         if (strat == FWI_STORE_BINOMIAL) b += (size_t)nslots * nb * state * f;
         return b;
     }
 
+    // grow a buffer whose address is captured in graphs
+    int grow(DBuf& buf, size_t n) {
+        if (buf.p && n <= buf.bytes) return FWI_OK;
+        drop_graphs();
+        return buf.ensure(n);
+    }
+
+    struct TileSet {
+        DBuf buf;
+        int ntiles = 0, bx = 0, tz = 0, grid_sf = 1, grid_sa = 1, grid_v = 1;
+    };
+    std::map<int, std::unique_ptr<TileSet>> tilesets;  // by batch size
+    int Bcap = 0;
+    size_t rows_cap = 0;
+    DBuf d_obsf, d_rowrec, d_gacc;
+
+    int tiles_for(int nb) {
+        auto& ts = tilesets[nb];
+        if (!ts) ts.reset(new TileSet());
+        if (ts->ntiles == 0) {
+            std::vector<Tile> t;
+            plan_tiles(nb, t);
+            FWI_TRY(grow(ts->buf, t.size() * sizeof(Tile)));
+            CUDA_TRY(cudaMemcpyAsync(ts->buf.p, t.data(), t.size() * sizeof(Tile), cudaMemcpyHostToDevice,
+                                     stream));
+            ts->ntiles = (int)t.size();
+            ts->bx = bx;
+            ts->tz = tz;
+            // persistent grids: resident capacity, never more blocks than tiles
+            ts->grid_sf = std::max(1, std::min(ts->ntiles, num_sms * std::max(1, ks.occ_f())));
+            ts->grid_sa = std::max(1, std::min(ts->ntiles, num_sms * std::max(1, ks.occ_a())));
+            ts->grid_v = std::max(1, std::min(ts->ntiles, num_sms * std::max(1, ks.occ_v())));
+        }
+        ntiles = ts->ntiles;
+        bx = ts->bx;
+        tz = ts->tz;
+        grid_sf = ts->grid_sf;
+        grid_sa = ts->grid_sa;
+        grid_v = ts->grid_v;
+        d_tiles_p = ts->buf.as<Tile>();
+        return FWI_OK;
+    }
+    const Tile* d_tiles_p = nullptr;
+
+    int slots_for(int nb, bool keep, int* out) {
+        *out = 0;
+        if (!(keep && strategy == FWI_STORE_BINOMIAL)) return FWI_OK;
+        size_t bud = budget;
+        if (bud == 0) {
+            size_t fr = 0, tot = 0;
+            CUDA_TRY(cudaMemGetInfo(&fr, &tot));
+            bud = (size_t)(0.9 * (double)(fr + allocated_bytes()));
+        }
+        const int cap = std::max(Bcap, nb);
+        const size_t base = batch_bytes(cap, 0, FWI_STORE_BINOMIAL) + fixed_bytes();
+        const size_t per_slot = (size_t)cap * state * 4;
+        long long fit = bud > base ? (long long)((bud - base) / per_slot) : 0;
+        int want = 0;
+        if (snapshots_req > 0) {
+            if (fit < std::min(snapshots_req, nft - 1))
+                return fail(FWI_ERR_NOMEM, "budget too small for " + std::to_string(snapshots_req) +
+                                               " checkpoints per shot");
+            want = snapshots_req;
+        } else {
+            want = (int)std::min<long long>(fit, nft - 1);
+        }
+        *out = std::max(0, std::min(want, nft - 1));
+        return FWI_OK;
+    }
+
     int setup_batch(int nb, const int* ids, bool keep) {
         if (!have_model) return fail(FWI_ERR_STATE, "set a model first");
         if (nb < 1 || !ids) return fail(FWI_ERR_INVALID, "empty shot batch");
-        std::vector<int> s(ids, ids + nb);
-        const bool same = (nb == B && s == shots);
-        // checkpoint slots
         int want_slots = 0;
-        if (keep && strategy == FWI_STORE_BINOMIAL) {
-            size_t bud = budget;
-            if (bud == 0) {
-                size_t fr = 0, tot = 0;
-                CUDA_TRY(cudaMemGetInfo(&fr, &tot));
-                bud = (size_t)(0.9 * (double)(fr + allocated_bytes()));
-            }
-            const size_t base = batch_bytes(nb, 0, FWI_STORE_BINOMIAL) + fixed_bytes();
-            const size_t per_slot = (size_t)nb * state * 4;
-            long long fit = bud > base ? (long long)((bud - base) / per_slot) : 0;
-            if (snapshots_req > 0) {
-                if (fit < snapshots_req)
-                    return fail(FWI_ERR_NOMEM, "budget too small for " + std::to_string(snapshots_req) +
-                                                   " checkpoints per shot");
-                want_slots = snapshots_req;
-            } else {
-                want_slots = (int)std::min<long long>(fit, nft - 1);
-            }
-            want_slots = std::max(0, std::min(want_slots, nft - 1));
-        }
-        if (same && want_slots == slots && !tiles_dirty) return FWI_OK;
-        drop_graphs();
+        FWI_TRY(slots_for(nb, keep, &want_slots));
+        const int cap = std::max(Bcap, nb);
+        if (budget > 0 && batch_bytes(cap, want_slots, keep ? strategy : -1) + fixed_bytes() > budget)
+            return fail(FWI_ERR_NOMEM, "batch does not fit the memory budget");
+        // receiver rows of this batch
+        std::vector<int> nrows_v, nslot_v;
+        for (int b = 0; b < nb; b++)
+            for (int r = 0; r < nrec; r++)
+                if (rshot[r] == ids[b] && rcomp[r] == 2) {
+                    nrows_v.push_back(r);
+                    nslot_v.push_back(b);
+                }
+        const size_t nrows = nrows_v.size();
+        // buffers (capacity; addresses captured in graphs)
+        FWI_TRY(grow(d_fwd, (size_t)cap * state * 4));
+        FWI_TRY(grow(d_adj, (size_t)cap * state * 4));
+        FWI_TRY(grow(d_ws, (size_t)cap * field * 4));
+        FWI_TRY(grow(d_wr, (size_t)cap * field * 4));
+        FWI_TRY(grow(d_ux, (size_t)cap * field * 4));
+        FWI_TRY(grow(d_uz, (size_t)cap * field * 4));
+        FWI_TRY(grow(d_grad, (size_t)cap * 3 * nf * 4));
+        FWI_TRY(grow(d_gsum, (size_t)3 * nf * 4));
+        FWI_TRY(grow(d_gacc, (size_t)3 * nf * 4));
+        if (keep && strategy == FWI_STORE_FULL) FWI_TRY(grow(d_store, (size_t)cap * nft * 5 * nf * 4));
+        if (keep && strategy == FWI_STORE_BINOMIAL && want_slots > 0)
+            FWI_TRY(grow(d_snap, (size_t)want_slots * cap * state * 4));
+        rows_cap = std::max(rows_cap, std::max<size_t>(1, nrows));
+        FWI_TRY(grow(d_rec, rows_cap * nt * 4));
+        FWI_TRY(grow(d_resid, rows_cap * nt * 4));
+        FWI_TRY(grow(d_rowmis, rows_cap * 8));
+        FWI_TRY(grow(d_rowrec, rows_cap * 4));
+        FWI_TRY(grow(d_blow, 16));
+        FWI_TRY(grow(d_obsf, std::max<size_t>(1, (size_t)nrec) * nt * 4));
+        FWI_TRY(grow(d_items_f, (size_t)cap * sizeof(ItemDesc)));
+        FWI_TRY(grow(d_items_a, (size_t)cap * sizeof(ItemDesc)));
+        Bcap = cap;
+        B = nb;
+        shots.assign(ids, ids + nb);
+        slots = want_slots;
+        rows = nrows_v;
+        row_slot = nslot_v;
         fwd_kept = false;
         bwd_done = false;
-        obs_valid = false;
-        if (budget > 0 && batch_bytes(nb, want_slots, keep ? strategy : -1) + fixed_bytes() > budget)
-            return fail(FWI_ERR_NOMEM, "batch does not fit the memory budget");
-        B = nb;
-        shots = s;
-        slots = want_slots;
-        // buffers
-        FWI_TRY(d_fwd.ensure((size_t)B * state * 4));
-        FWI_TRY(d_adj.ensure((size_t)B * state * 4));
-        FWI_TRY(d_ws.ensure((size_t)B * field * 4));
-        FWI_TRY(d_wr.ensure((size_t)B * field * 4));
-        FWI_TRY(d_ux.ensure((size_t)B * field * 4));
-        FWI_TRY(d_uz.ensure((size_t)B * field * 4));
-        FWI_TRY(d_grad.ensure((size_t)B * 3 * nf * 4));
-        FWI_TRY(d_gsum.ensure((size_t)3 * nf * 4));
-        if (keep && strategy == FWI_STORE_FULL) FWI_TRY(d_store.ensure((size_t)B * nft * 5 * nf * 4));
-        if (keep && strategy == FWI_STORE_BINOMIAL && slots > 0)
-            FWI_TRY(d_snap.ensure((size_t)slots * B * state * 4));
-        // receiver rows of this batch
-        rows.clear();
-        row_slot.clear();
-        std::vector<int> slot_of_row;
-        for (int b = 0; b < B; b++)
-            for (int r = 0; r < nrec; r++)
-                if (rshot[r] == shots[b] && rcomp[r] == 2) {
-                    rows.push_back(r);
-                    row_slot.push_back(b);
-                }
-        const size_t nrows = rows.size();
-        FWI_TRY(d_rec.ensure(std::max<size_t>(1, nrows) * nt * 4));
-        FWI_TRY(d_obs.ensure(std::max<size_t>(1, nrows) * nt * 4));
-        FWI_TRY(d_resid.ensure(std::max<size_t>(1, nrows) * nt * 4));
-        FWI_TRY(d_rowmis.ensure(std::max<size_t>(1, nrows) * 8));
-        FWI_TRY(d_blow.ensure(16));
         // events per slot, grouped by column, sorted by (z, inject-before-record, index)
         struct Ev { int x, z, kind, idx, code; };
         std::vector<int> colf((size_t)B * (nxt + 1)), cola((size_t)B * (nxt + 1));
@@ -529,19 +611,19 @@ struct Engine {
             std::sort(ef.begin(), ef.end(), cmp);
             std::sort(ea.begin(), ea.end(), cmp);
             auto fill = [&](std::vector<Ev>& ev, std::vector<int>& col, std::vector<int2>& flat) {
-                const size_t base = flat.size();
+                const int base = (int)flat.size();
                 int* c = col.data() + (size_t)b * (nxt + 1);
                 size_t k = 0;
                 for (int x = 0; x <= nxt; x++) {
                     while (k < ev.size() && ev[k].x < x) k++;
-                    c[x] = (int)(k);  // relative; rebased below
+                    c[x] = base + (int)k;
                 }
                 for (auto& e : ev) flat.push_back(make_int2(e.z, e.code));
-                for (int x = 0; x <= nxt; x++) c[x] += (int)base;
             };
             fill(ef, colf, evf);
             fill(ea, cola, eva);
         }
+        // event tables are reached through the item descriptors only (not captured)
         FWI_TRY(d_evcol_f.ensure(colf.size() * 4));
         FWI_TRY(d_evcol_a.ensure(cola.size() * 4));
         FWI_TRY(d_ev_f.ensure(std::max<size_t>(1, evf.size()) * 8));
@@ -552,37 +634,56 @@ struct Engine {
             CUDA_TRY(cudaMemcpyAsync(d_ev_f.p, evf.data(), evf.size() * 8, cudaMemcpyHostToDevice, stream));
         if (!eva.empty())
             CUDA_TRY(cudaMemcpyAsync(d_ev_a.p, eva.data(), eva.size() * 8, cudaMemcpyHostToDevice, stream));
-        // item descriptors
+        if (nrows)
+            CUDA_TRY(cudaMemcpyAsync(d_rowrec.p, rows.data(), nrows * 4, cudaMemcpyHostToDevice, stream));
         std::vector<ItemDesc> itf(B), ita(B);
         for (int b = 0; b < B; b++) {
             fill_item(itf[b], b, false);
             fill_item(ita[b], b, true);
         }
-        FWI_TRY(d_items_f.ensure(B * sizeof(ItemDesc)));
-        FWI_TRY(d_items_a.ensure(B * sizeof(ItemDesc)));
         CUDA_TRY(cudaMemcpyAsync(d_items_f.p, itf.data(), B * sizeof(ItemDesc), cudaMemcpyHostToDevice, stream));
         CUDA_TRY(cudaMemcpyAsync(d_items_a.p, ita.data(), B * sizeof(ItemDesc), cudaMemcpyHostToDevice, stream));
-        std::vector<Tile> t;
-        plan_tiles(B, t);
-        ntiles = (int)t.size();
-        // persistent grids: resident capacity, never more blocks than tiles
-        grid_sf = std::max(1, std::min(ntiles, num_sms * std::max(1, ks.occ_f(bx))));
-        grid_sa = std::max(1, std::min(ntiles, num_sms * std::max(1, ks.occ_a(bx))));
-        grid_v = std::max(1, std::min(ntiles, num_sms * std::max(1, ks.occ_v(bx))));
-        FWI_TRY(d_tiles.ensure(t.size() * sizeof(Tile)));
-        CUDA_TRY(cudaMemcpyAsync(d_tiles.p, t.data(), t.size() * sizeof(Tile), cudaMemcpyHostToDevice, stream));
+        FWI_TRY(tiles_for(B));
         CUDA_TRY(cudaStreamSynchronize(stream));
-        tiles_dirty = false;
         if (keep && strategy == FWI_STORE_BINOMIAL) plan = plan_binomial(nft, slots, &plan_cost);
         return FWI_OK;
     }
-    bool tiles_dirty = false;
+    std::string shape_key() const {
+        return "|B" + std::to_string(B) + "|r" + std::to_string(rows.size()) + "|s" +
+               std::to_string(slots) + "|st" + std::to_string(strategy) + "|t" + std::to_string(ntiles) +
+               "|g" + std::to_string(grad_on ? 1 : 0);
+    }
+
+    // FP64 host observed data -> resident FP32 rows [nrec][nt] for the given receivers.
+    int upload_obs(const double* obs, const std::vector<int>& recs) {
+        if (recs.empty()) return FWI_OK;
+        FWI_TRY(grow(d_obsf, std::max<size_t>(1, (size_t)nrec) * nt * 4));
+        FWI_TRY(h_stage.ensure(recs.size() * nt * 4));
+        float* o = h_stage.as<float>();
+        for (size_t k = 0; k < recs.size(); k++)
+            for (int t = 0; t < nt; t++) o[k * nt + t] = (float)obs[(size_t)recs[k] * nt + t];
+        // one copy per run of consecutive receiver indices
+        size_t k = 0;
+        while (k < recs.size()) {
+            size_t j = k + 1;
+            while (j < recs.size() && recs[j] == recs[j - 1] + 1) j++;
+            CUDA_TRY(cudaMemcpyAsync(d_obsf.as<float>() + (size_t)recs[k] * nt, o + k * nt,
+                                     (j - k) * nt * 4, cudaMemcpyHostToDevice, stream));
+            k = j;
+        }
+        CUDA_TRY(cudaStreamSynchronize(stream));
+        obs_valid = true;
+        last_h2d = (int64_t)(recs.size() * nt * 4);
+        return FWI_OK;
+    }
+    int64_t last_h2d = 0;
 
     size_t fixed_bytes() const { return d_mat.bytes + d_cpml.bytes + d_srcsig.bytes; }
     size_t allocated_bytes() const {
-        return d_fwd.bytes + d_adj.bytes + d_ws.bytes + d_wr.bytes + d_ux.bytes + d_uz.bytes +
-               d_grad.bytes + d_gsum.bytes + d_store.bytes + d_snap.bytes + d_rec.bytes +
-               d_obs.bytes + d_resid.bytes;
+        size_t t = d_fwd.bytes + d_adj.bytes + d_ws.bytes + d_wr.bytes + d_ux.bytes + d_uz.bytes +
+                   d_grad.bytes + d_gsum.bytes + d_gacc.bytes + d_store.bytes + d_snap.bytes +
+                   d_rec.bytes + d_obsf.bytes + d_resid.bytes;
+        return t;
     }
 
     void fill_item(ItemDesc& d, int b, bool adj) {
@@ -634,12 +735,24 @@ struct Engine {
 
     // ---- launches ----------------------------------------------------------
     void step(bool adj, int it, unsigned sflags, unsigned vflags) {
-        const dim3 b(bx);
         const ItemDesc* items = adj ? d_items_a.as<ItemDesc>() : d_items_f.as<ItemDesc>();
-        const Tile* tl = d_tiles.as<Tile>();
-        (adj ? ks.stress_a : ks.stress_f)(dim3(adj ? grid_sa : grid_sf), b, stream, items, tl, ntiles, it, sflags);
-        ks.velocity(dim3(grid_v), b, stream, items, tl, ntiles, it, vflags);
+        const Tile* tl = d_tiles_p;
+        int* err = d_err.as<int>();
+        (adj ? ks.stress_a : ks.stress_f)(dim3(adj ? grid_sa : grid_sf), stream, items, tl, ntiles, it, sflags, err);
+        ks.velocity(dim3(grid_v), stream, items, tl, ntiles, it, vflags, err);
         launches_now += 2;
+    }
+
+    // Error flags raised by the kernels (a bounded wait that timed out).
+    int check_kernel_flags() {
+        int h = 0;
+        CUDA_TRY(cudaMemcpy(&h, d_err.p, sizeof(int), cudaMemcpyDeviceToHost));
+        if (h) {
+            cudaMemset(d_err.p, 0, sizeof(int));
+            return fail(FWI_ERR_CUDA, "a kernel's shared-memory pipeline wait timed out (flag " +
+                                          std::to_string(h) + "); results discarded");
+        }
+        return FWI_OK;
     }
 
     // forward steps [t0, t1) of the working forward state
@@ -704,17 +817,11 @@ struct Engine {
         const bool resident = (flags & FWI_FWD_RESIDENT_OBS) != 0;
         FWI_TRY(setup_batch(nb, ids, keep != 0));
         if (resident && !obs_valid)
-            return fail(FWI_ERR_STATE, "no observed data resident for this batch");
+            return fail(FWI_ERR_STATE, "no observed data resident on the device");
         const size_t nrows = rows.size();
         const bool obs = resident || obs_in != nullptr;  // misfit + residual wanted
-        if (obs_in && !resident && nrows) {
-            FWI_TRY(h_stage.ensure(nrows * nt * 4));
-            float* o = h_stage.as<float>();
-            for (size_t k = 0; k < nrows; k++)
-                for (int t = 0; t < nt; t++) o[k * nt + t] = (float)obs_in[(size_t)rows[k] * nt + t];
-            CUDA_TRY(cudaMemcpyAsync(d_obs.p, o, nrows * nt * 4, cudaMemcpyHostToDevice, stream));
-            obs_valid = true;
-        }
+        last_h2d = 0;
+        if (obs_in && !resident) FWI_TRY(upload_obs(obs_in, rows));
         cudaEvent_t e0, e1;
         CUDA_TRY(cudaEventCreate(&e0));
         CUDA_TRY(cudaEventCreate(&e1));
@@ -730,8 +837,7 @@ struct Engine {
                 if (a.kind == Action::SAVE) saves.push_back({a.b, a.a});
             }
         const std::string key = std::string("fwd") + (store ? "S" : "") + (ckpt ? "C" : "") +
-                                (obs ? "O" : "");
-        (void)obs_in;
+                                (obs ? "O" : "") + shape_key();
         FWI_TRY(run_phase(key, [&]() -> int {
             CUDA_TRY(cudaMemsetAsync(d_fwd.p, 0, (size_t)B * state * 4, stream));
             CUDA_TRY(cudaMemsetAsync(d_ws.p, 0, (size_t)B * field * 4, stream));
@@ -746,8 +852,8 @@ struct Engine {
             if (obs && nrows) {
                 CUDA_TRY(cudaMemsetAsync(d_blow.p, 0, 4, stream));
                 residual_kernel<<<(unsigned)nrows, 256, 0, stream>>>(
-                    d_rec.as<float>(), d_obs.as<float>(), d_resid.as<float>(), d_rowmis.as<double>(),
-                    d_blow.as<int>(), nt, 0.5 * dt);
+                    d_rec.as<float>(), d_obsf.as<float>(), d_rowrec.as<int>(), d_resid.as<float>(),
+                    d_rowmis.as<double>(), d_blow.as<int>(), nt, 0.5 * dt);
                 launches_now++;
             }
             return FWI_OK;
@@ -768,6 +874,7 @@ struct Engine {
         cudaEventElapsedTime(&ms, e0, e1);
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
+        FWI_TRY(check_kernel_flags());
         stats.last_forward_ms = ms;
         stats.launches = launches_now;
         stats.forward_steps = (int64_t)nt;
@@ -778,7 +885,7 @@ struct Engine {
         if (rec_out)
             for (size_t k = 0; k < nrows; k++)
                 for (int t = 0; t < nt; t++) rec_out[(size_t)rows[k] * nt + t] = (double)rec[k * nt + t];
-        stats.h2d_bytes = (obs_in && !resident) ? (int64_t)(nrows * nt * 4) : 0;
+        stats.h2d_bytes = last_h2d;
         stats.d2h_bytes = (int64_t)((rec_out ? nrows * nt * 4 : 0) + (obs ? nrows * 8 + 4 : 0));
         if (misfit) {
             for (int b = 0; b < B; b++) misfit[b] = 0.0;
@@ -800,8 +907,8 @@ struct Engine {
         cudaEvent_t a, b;
         CUDA_TRY(cudaEventCreate(&a));
         CUDA_TRY(cudaEventCreate(&b));
-        const dim3 blk(bx);
-        const Tile* tl = d_tiles.as<Tile>();
+        const Tile* tl = d_tiles_p;
+        int* er = d_err.as<int>();
         const ItemDesc* itf = d_items_f.as<ItemDesc>();
         const ItemDesc* ita = d_items_a.as<ItemDesc>();
         const bool have_adj_src = strategy != FWI_STORE_BINOMIAL ? d_store.p != nullptr : true;
@@ -810,10 +917,10 @@ struct Engine {
             if (adj && !have_adj_src) { ms[k] = 0.0; continue; }
             const int it = fwi_dt * (nft - 1);  // a sampled step: the gradient runs
             auto launch = [&]() {
-                if (k == 0) ks.stress_f(dim3(grid_sf), blk, stream, itf, tl, ntiles, it, 0u);
-                if (k == 1) ks.velocity(dim3(grid_v), blk, stream, itf, tl, ntiles, it, FL_INJECT | FL_WE);
-                if (k == 2) ks.stress_a(dim3(grid_sa), blk, stream, ita, tl, ntiles, it, FL_GRAD);
-                if (k == 3) ks.velocity(dim3(grid_v), blk, stream, ita, tl, ntiles, it, FL_INJECT | FL_WE);
+                if (k == 0) ks.stress_f(dim3(grid_sf), stream, itf, tl, ntiles, it, 0u, er);
+                if (k == 1) ks.velocity(dim3(grid_v), stream, itf, tl, ntiles, it, FL_INJECT | FL_WE, er);
+                if (k == 2) ks.stress_a(dim3(grid_sa), stream, ita, tl, ntiles, it, FL_GRAD, er);
+                if (k == 3) ks.velocity(dim3(grid_v), stream, ita, tl, ntiles, it, FL_INJECT | FL_WE, er);
             };
             launch();  // warm-up
             CUDA_TRY(cudaEventRecord(a, stream));
@@ -832,7 +939,7 @@ struct Engine {
     }
 
     // ---- backward --------------------------------------------------------------
-    int backward(double* gl, double* gm, double* gr, int sum_shots) {
+    int backward(double* gl, double* gm, double* gr, int sum_shots, bool accumulate = false) {
         FWI_TRY(bind());
         if (!fwd_kept) return fail(FWI_ERR_NOFORWARD, "backward needs a forward(keep=1)");
         if (!have_resid) return fail(FWI_ERR_STATE, "backward needs observed data (forward obs) or a loaded residual");
@@ -844,7 +951,7 @@ struct Engine {
         launches_now = 0;
         long long recompute = 0;
         CUDA_TRY(cudaEventRecord(e0, stream));
-        const std::string key = strategy == FWI_STORE_BINOMIAL ? "bwdC" : "bwdS";
+        const std::string key = std::string(strategy == FWI_STORE_BINOMIAL ? "bwdC" : "bwdS") + shape_key();
         FWI_TRY(run_phase(key, [&]() -> int {
             CUDA_TRY(cudaMemsetAsync(d_adj.p, 0, (size_t)B * state * 4, stream));
             CUDA_TRY(cudaMemsetAsync(d_wr.p, 0, (size_t)B * field * 4, stream));
@@ -891,14 +998,17 @@ struct Engine {
             }
             return FWI_OK;
         }));
-        if (sum_shots && B > 1) {
-            sum_shots_kernel<<<592, 256, 0, stream>>>(d_grad.as<float>(), d_gsum.as<float>(), 3 * nf, B);
+        if (accumulate) {
+            sum_shots_kernel<<<592, 256, 0, stream>>>(d_grad.as<float>(), d_gacc.as<float>(), 3 * nf, B, 1);
+            launches_now++;
+        } else if (sum_shots && B > 1) {
+            sum_shots_kernel<<<592, 256, 0, stream>>>(d_grad.as<float>(), d_gsum.as<float>(), 3 * nf, B, 0);
             launches_now++;
         }
         CUDA_TRY(cudaEventRecord(e1, stream));
         const bool summed = sum_shots && B > 1;
         const size_t ntrip = summed ? 1 : (size_t)B;
-        const bool want = gl || gm || gr;
+        const bool want = !accumulate && (gl || gm || gr);
         FWI_TRY(h_grad.ensure(want ? ntrip * 3 * nf * 4 : 16));
         const float* g = h_grad.as<float>();
         if (want)
@@ -911,6 +1021,7 @@ struct Engine {
         cudaEventElapsedTime(&ms, e0, e1);
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
+        FWI_TRY(check_kernel_flags());
         stats.last_backward_ms = ms;
         stats.launches = launches_now;
         stats.adjoint_steps = nt;
@@ -925,6 +1036,78 @@ struct Engine {
                 if (gr) gr[s * nf + i] = t[2 * nf + i];
             }
         bwd_done = true;
+        return FWI_OK;
+    }
+
+    // ---- gradient over many shots in sub-batches --------------------------------
+    int batch_override = 0;
+
+    // Shots per launch: enough cells per launch to fill the GPU with a few
+    // waves of blocks (about 8 M cells; measured on the 1068x568 grid, order
+    // 8: 3.5 shot-gradients/s at 4 shots per launch, 3.8 at 8-16, 3.6 at 64).
+    int auto_batch(int n) const {
+        const double cells = (double)(nxt - 2 * fpad) * (double)(nzt - 2 * fpad);
+        const int b = (int)std::ceil(8.0e6 / std::max(1.0, cells));
+        return std::max(1, std::min(n, b));
+    }
+
+    int gradient(int n, const int* ids, const double* obs, double* misfit, double* gl, double* gm,
+                 double* gr, int flags) {
+        FWI_TRY(bind());
+        if (n < 1 || !ids) return fail(FWI_ERR_INVALID, "empty shot list");
+        const bool resident = (flags & FWI_FWD_RESIDENT_OBS) != 0;
+        if (!resident && !obs) return fail(FWI_ERR_INVALID, "observed data required");
+        if (resident && !obs_valid) return fail(FWI_ERR_STATE, "no observed data resident on the device");
+        if (!resident) {
+            std::vector<int> recs;
+            for (int r = 0; r < nrec; r++) {
+                if (rcomp[r] != 2) continue;
+                for (int b = 0; b < n; b++)
+                    if (rshot[r] == ids[b]) { recs.push_back(r); break; }
+            }
+            FWI_TRY(upload_obs(obs, recs));
+        }
+        const int64_t h2d = resident ? 0 : last_h2d;
+        const int bs = batch_override > 0 ? std::min(batch_override, n) : auto_batch(n);
+        CUDA_TRY(cudaMemsetAsync(d_gacc.p ? d_gacc.p : nullptr, 0, d_gacc.p ? 3 * nf * 4 : 0, stream));
+        double fwd_ms = 0, bwd_ms = 0;
+        int64_t launches = 0, recompute = 0;
+        std::vector<double> mis(bs);
+        for (int k = 0; k < n; k += bs) {
+            const int m = std::min(bs, n - k);
+            FWI_TRY(forward(m, ids + k, nullptr, nullptr, mis.data(), FWI_FWD_KEEP | FWI_FWD_RESIDENT_OBS));
+            if (misfit) std::copy(mis.begin(), mis.begin() + m, misfit + k);
+            if (k == 0) CUDA_TRY(cudaMemsetAsync(d_gacc.p, 0, 3 * nf * 4, stream));
+            fwd_ms += stats.last_forward_ms;
+            launches += stats.launches;
+            FWI_TRY(backward(nullptr, nullptr, nullptr, 1, true));
+            bwd_ms += stats.last_backward_ms;
+            launches += stats.launches;
+            recompute += stats.recompute_steps;
+        }
+        const bool want = gl || gm || gr;
+        FWI_TRY(h_grad.ensure(want ? 3 * nf * 4 : 16));
+        if (want)
+            CUDA_TRY(cudaMemcpyAsync(h_grad.p, d_gacc.p, 3 * nf * 4, cudaMemcpyDeviceToHost, stream));
+        CUDA_TRY(cudaStreamSynchronize(stream));
+        const float* g = h_grad.as<float>();
+        for (size_t i = 0; want && i < nf; i++) {
+            if (gl) gl[i] = g[i];
+            if (gm) gm[i] = g[nf + i];
+            if (gr) gr[i] = g[2 * nf + i];
+        }
+        stats.last_forward_ms = fwd_ms;
+        stats.last_backward_ms = bwd_ms;
+        stats.launches = launches;
+        // per shot (every sub-batch runs the same schedule)
+        const int nsub = (n + bs - 1) / bs;
+        stats.forward_steps = (int64_t)nt;
+        stats.recompute_steps = recompute / nsub;
+        stats.adjoint_steps = (int64_t)nt;
+        stats.h2d_bytes = h2d;
+        stats.d2h_bytes = (misfit ? 0 : 0) + (want ? (int64_t)(3 * nf * 4) : 0) +
+                          (int64_t)(rows_cap * 8) * ((n + bs - 1) / bs);
+        stats.batch = bs;
         return FWI_OK;
     }
 
@@ -1213,15 +1396,23 @@ int fwi_psv_set_gradient_mode(fwi_psv_engine* h, int mode) {
     return FWI_OK;
 }
 
-int fwi_psv_set_exec(fwi_psv_engine* h, int use_graphs, int block_x, int tile_z) {
+int fwi_psv_set_exec(fwi_psv_engine* h, int use_graphs, int block_x, int tile_z, int batch) {
     GUARD_ENGINE(h);
-    if (block_x < 0 || block_x > 256 || (block_x % 32) != 0 || tile_z < 0)
-        return fail(FWI_ERR_INVALID, "block_x must be a multiple of 32 in 32..256, tile_z >= 0");
+    if ((block_x != 0 && block_x != 32 && block_x != fwi::kTileX) || tile_z < 0 || batch < 0)
+        return fail(FWI_ERR_INVALID, "block_x must be 0, 32 or 128; tile_z and batch >= 0");
     Engine& e = h->e;
     e.use_graphs = use_graphs ? 1 : 0;
     e.bx_req = block_x;
     e.tz_req = tile_z;
-    e.tiles_dirty = true;
+    e.batch_override = batch;
+    // block_x 128 (or a tile height) selects the z-march, block_x 32 the scalar
+    // cell mapping, 0 the default vectorised cells
+    const int map = (block_x == fwi::kTileX || tile_z > 0) ? 0 : (block_x == 32 ? 1 : 2);
+    if (map != e.kmap) {
+        e.kmap = map;
+        e.ks = fwi::kernels_for(e.fpad, map);
+    }
+    for (auto& kv : e.tilesets) kv.second->ntiles = 0;
     e.drop_graphs();
     return FWI_OK;
 }
@@ -1230,6 +1421,12 @@ int fwi_psv_forward(fwi_psv_engine* h, int nshots, const int* shots, const doubl
                     double* rec_out, double* misfit, int flags) {
     GUARD_ENGINE(h);
     return h->e.forward(nshots, shots, obs, rec_out, misfit, flags);
+}
+
+int fwi_psv_gradient(fwi_psv_engine* h, int nshots, const int* shots, const double* obs,
+                     double* misfit, double* gl, double* gm, double* gr, int flags) {
+    GUARD_ENGINE(h);
+    return h->e.gradient(nshots, shots, obs, misfit, gl, gm, gr, flags);
 }
 
 int fwi_psv_backward(fwi_psv_engine* h, double* gl, double* gm, double* gr, int sum_shots) {

@@ -88,8 +88,8 @@ class Engine:
         s = STRATEGIES[strategy] if isinstance(strategy, str) else int(strategy)
         check(_capi.lib().fwi_psv_set_strategy(self.h, s, snapshots, budget_bytes), "set_strategy")
 
-    def set_exec(self, use_graphs=True, block_x=0, tile_z=0):
-        check(_capi.lib().fwi_psv_set_exec(self.h, int(use_graphs), block_x, tile_z), "set_exec")
+    def set_exec(self, use_graphs=True, block_x=0, tile_z=0, batch=0):
+        check(_capi.lib().fwi_psv_set_exec(self.h, int(use_graphs), block_x, tile_z, batch), "set_exec")
 
     def set_stream(self, stream_handle: int | None):
         check(_capi.lib().fwi_psv_set_stream(self.h, C.c_void_p(stream_handle or 0)), "set_stream")
@@ -121,6 +121,18 @@ class Engine:
         if sum_shots:
             g = [x[0] for x in g]
         return tuple(g)
+
+    def gradient(self, shots, obs=None, resident=False, want=True):
+        """Summed shot gradients (lam, mu, rho) [nfz][nfx] and per-shot misfits,
+        computed in sub-batches on the device (fwi_psv_gradient)."""
+        shots = _i32(np.atleast_1d(shots))
+        mis = np.zeros(len(shots))
+        g = [np.zeros((self.nfz, self.nfx)) for _ in range(3)] if want else [None] * 3
+        o = _f64(obs) if (obs is not None and not resident) else None
+        flags = _capi.FWI_FWD_RESIDENT_OBS if resident else 0
+        check(_capi.lib().fwi_psv_gradient(self.h, len(shots), pi(shots), pd(o), pd(mis),
+                                           *[pd(x) for x in g], flags), "gradient")
+        return (tuple(g) if want else None), mis
 
     def time_kernels(self, reps=20):
         """Average device ms of one launch of: forward stress, forward velocity,

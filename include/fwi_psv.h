@@ -172,6 +172,17 @@ int fwi_psv_forward(fwi_psv_engine* e, int nshots, const int* shots, const doubl
 int fwi_psv_backward(fwi_psv_engine* e, double* grad_lam, double* grad_mu, double* grad_rho,
                      int sum_shots);
 
+/* Shot gradients of `nshots` shots summed into grad_* ([nfz][nfx] each; any
+ * may be NULL), with misfit[nshots] (or NULL).  The shots run in sub-batches
+ * (FWI_FWD_* flags apply; the batch size is set by fwi_psv_set_exec or chosen
+ * so a sub-batch's working set stays in L2): per sub-batch a forward sweep
+ * with checkpoints or storage, the residual against obs ([nrec][nt]), the
+ * backward, and a device-side sum.  The gradients stay on the device until
+ * the end; one host transfer of the sum. */
+int fwi_psv_gradient(fwi_psv_engine* e, int nshots, const int* shots, const double* obs,
+                     double* misfit, double* grad_lam, double* grad_mu, double* grad_rho,
+                     int flags);
+
 /* Energy sums of the last forward (Ws) and backward (Wr) for shot slot `slot`
  * of the batch, [nzt][nxt] (the reference's We arrays). */
 int fwi_psv_energy(fwi_psv_engine* e, int slot, double* Ws, double* Wr);
@@ -181,13 +192,15 @@ int fwi_psv_energy(fwi_psv_engine* e, int slot, double* Ws, double* Wr);
 int fwi_psv_wavefield(fwi_psv_engine* e, int which, int slot, double* vx, double* vz,
                       double* sxx, double* szx, double* szz);
 
-/* Counters of the last forward/backward: kernel launches, time steps
- * advanced (forward + recompute), adjoint steps, and device bytes held. */
+/* Counters of the last forward/backward/gradient call: kernel launches, time
+ * steps of the recording forward sweep, of recomputation and of the adjoint
+ * (per shot for fwi_psv_gradient), and device bytes held. */
 typedef struct fwi_psv_stats {
     int64_t launches, forward_steps, recompute_steps, adjoint_steps;
     int64_t device_bytes, snapshots;
     double last_forward_ms, last_backward_ms;  /* device time of the compute (CUDA events) */
     int64_t h2d_bytes, d2h_bytes;              /* host<->device bytes of the last call */
+    int64_t batch;                             /* shots per launch of the last gradient call */
 } fwi_psv_stats;
 int fwi_psv_get_stats(fwi_psv_engine* e, fwi_psv_stats* out);
 
@@ -209,8 +222,9 @@ int fwi_psv_checkpoint_plan(int nsteps, int slots, int* actions, int cap, int* c
 int fwi_psv_time_kernels(fwi_psv_engine* e, int reps, double ms[4]);
 
 /* Execution options: use_graphs != 0 captures the time loop in CUDA graphs
- * (default 1); block_x / tile_z override the autotuned tile (0 = auto). */
-int fwi_psv_set_exec(fwi_psv_engine* e, int use_graphs, int block_x, int tile_z);
+ * (default 1); block_x (0 or 128, the tile width) and tile_z (rows per tile)
+ * set the tile shape; batch = shots per launch of fwi_psv_gradient (0 = automatic). */
+int fwi_psv_set_exec(fwi_psv_engine* e, int use_graphs, int block_x, int tile_z, int batch);
 
 /* ---- reference-shaped calls --------------------------------------------- */
 

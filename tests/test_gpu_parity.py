@@ -162,12 +162,28 @@ def test_graphs_and_direct_launches_agree():
         assert np.array_equal(out[0][1][i], out[1][1][i])
 
 
-@pytest.mark.parametrize("bx,tz", [(32, 4), (64, 16), (128, 64), (256, 7)])
-def test_tile_shapes_bitwise_identical(bx, tz):
+@pytest.mark.parametrize("bx,tz", [(128, 1), (128, 5), (128, 64), (32, 0)])
+def test_thread_mappings_agree(bx, tz):
+    """z-march tiles of any height, the scalar cell mapping and the default
+    vectorised mapping compute the same stencil (rounding may differ)."""
     p, obs = _oracle_case(8, 0, (1, 1, 1), nt=100, seed=6)
     with Engine(p) as eng:
-        rec0, _ = eng.forward([0], obs)
+        rec0, _ = eng.forward([0], obs, keep=True)
+        g0 = eng.backward()
         eng.set_exec(True, bx, tz)
+        rec1, _ = eng.forward([0], obs, keep=True)
+        g1 = eng.backward()
+    assert rel_l2(rec1, rec0) <= 1e-6
+    for i in range(3):
+        assert rel_l2(g1[i], g0[i]) <= 1e-5
+
+
+def test_z_march_tile_heights_bitwise_identical():
+    p, obs = _oracle_case(8, 0, (1, 1, 1), nt=100, seed=6)
+    with Engine(p) as eng:
+        eng.set_exec(True, 128, 3)
+        rec0, _ = eng.forward([0], obs)
+        eng.set_exec(True, 128, 40)
         rec1, _ = eng.forward([0], obs)
     assert np.array_equal(rec0, rec1)
 
@@ -185,6 +201,9 @@ def test_error_paths():
         bad_x[0] = 0
         with pytest.raises(_capi.FwiError) as e:
             eng.set_sources(bad_x, p.src_z, p.src_comp, p.src_shot, p.src_signal)
+        assert e.value.code == "FWI_ERR_INVALID"
+        with pytest.raises(_capi.FwiError) as e:
+            eng.set_exec(True, 64, 0)
         assert e.value.code == "FWI_ERR_INVALID"
         with pytest.raises(_capi.FwiError) as e:
             eng.forward([0], obs * 1e12 + 1e11)
