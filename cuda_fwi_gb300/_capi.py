@@ -85,6 +85,8 @@ _SIGS = {
     "fwi_psv_wavefield": (C.c_int, [C.c_void_p, C.c_int, C.c_int, dp, dp, dp, dp, dp]),
     "fwi_psv_get_stats": (C.c_int, [C.c_void_p, C.POINTER(Stats)]),
     "fwi_psv_time_kernels": (C.c_int, [C.c_void_p, C.c_int, dp]),
+    "fwi_psv_misfit_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_double,
+                                         C.c_void_p, dp, C.c_void_p]),
     "fwi_psv_forward_kernel": (C.c_int, [C.c_int] * 6 + [C.c_double] * 3 + [C.c_int, C.c_int, dp, C.c_int]
                                + [dp] * 6 + [dp] * 5 + [C.c_int] + [dp] * 6 + [dp] * 8
                                + [C.c_int, ip, ip, ip, dp, ip] + [C.c_int, ip, ip, ip, dp, ip]

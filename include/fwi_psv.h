@@ -226,6 +226,27 @@ int fwi_psv_time_kernels(fwi_psv_engine* e, int reps, double ms[4]);
  * set the tile shape; batch = shots per launch of fwi_psv_gradient (0 = automatic). */
 int fwi_psv_set_exec(fwi_psv_engine* e, int use_graphs, int block_x, int tile_z, int batch);
 
+/* ---- allocation-free misfit ---------------------------------------------- */
+
+/* No counterpart in the reference (whose misfit, calculate_l2_adjoint_sources,
+ * runs on the host).  For callers that cannot allocate device memory from the
+ * code that evaluates the misfit: applications whose HBM is reserved up front
+ * by their own pool allocator, and time-critical loops where cudaMalloc/cudaFree
+ * would synchronise the device and stall other streams.  Given device-resident
+ * FP32 traces d_syn and d_obs ([nrows][nt]) it writes d_resid = syn - obs
+ * ([nrows][nt], FP32, difference taken in FP64) and *misfit = sum 0.5 dt diff^2
+ * (FP64, summed in trace order) on `stream` (a cudaStream_t, NULL = legacy
+ * default stream), then waits for the stream.  It allocates nothing: its
+ * scratch is a fixed device array of FWI_NOALLOC_MAX_ROWS traces that every GPU
+ * loading the library holds until exit; more traces return FWI_ERR_INVALID.
+ * The first call on a device looks up the array's address with that device
+ * current; make that first call before any stream capture.  All calls share
+ * the array: calls that overlap on the GPU race.  Returns FWI_ERR_DIVERGED when
+ * |diff| > 1e10, as the engine does. */
+#define FWI_NOALLOC_MAX_ROWS 65536
+int fwi_psv_misfit_noalloc(const float* d_syn, const float* d_obs, int nrows, int nt, double dt,
+                           float* d_resid, double* misfit, void* stream);
+
 /* ---- reference-shaped calls --------------------------------------------- */
 
 /* forward_kernel_PSV (fd_kernel.cuh:12-43) with flat FP64 host arrays in the
