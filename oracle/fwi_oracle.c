@@ -539,3 +539,298 @@ double orc_calc_opt_step(const double* L2, const double* sl) {
     }
     return -x[1] / (2.0 * x[2]);
 }
+
+/* ---------------------------------------------------------------------------
+ * Exact discrete adjoint (this oracle's own addition; the reference has no
+ * such mode).  It differentiates J = sum_it sum_r 0.5 dt (rec_r(it) - obs_r(it))^2
+ * of the time stepping above (stress_pass, velocity_pass, source injection,
+ * recording) with respect to lam, mu and rho, by transposing every statement
+ * of one step in reverse order and scattering each adjoint onto the cells the
+ * forward statement read.  Forward states come from sqrt(nt) checkpoints with
+ * per-segment recomputation, so memory stays at about 2 sqrt(nt) states.
+ * ------------------------------------------------------------------------- */
+
+typedef struct {
+    size_t n, nxs, nzs, total;
+} st_sizes;
+
+static st_sizes state_sizes(const orc_grid* g) {
+    st_sizes s;
+    s.n = (size_t)g->nzt * g->nxt;
+    s.nxs = (size_t)g->nzt * 2 * (g->npml + 1);
+    s.nzs = (size_t)2 * (g->npml + 1) * g->nxt;
+    s.total = 5 * s.n + 4 * s.nxs + 4 * s.nzs;
+    return s;
+}
+
+/* orc_wave view of one contiguous state block (We points to scratch). */
+static void wave_view(const orc_grid* g, double* base, double* we, orc_wave* w) {
+    st_sizes s = state_sizes(g);
+    w->vx = base; w->vz = base + s.n; w->sxx = base + 2 * s.n; w->szx = base + 3 * s.n;
+    w->szz = base + 4 * s.n;
+    double* x = base + 5 * s.n;
+    w->mem_vx_x = x; w->mem_vz_x = x + s.nxs; w->mem_sxx_x = x + 2 * s.nxs; w->mem_szx_x = x + 3 * s.nxs;
+    double* z = x + 4 * s.nxs;
+    w->mem_vx_z = z; w->mem_vz_z = z + s.nzs; w->mem_szz_z = z + 2 * s.nzs; w->mem_szx_z = z + 3 * s.nzs;
+    w->We = we;
+}
+
+static void fwd_step(const orc_grid* g, const orc_medium* m, orc_wave* w, int it, int ishot,
+                     const orc_seis* src, const double* src_signal) {
+    stress_pass(g, m, w);
+    velocity_pass(g, m, w);
+    for (int is = 0; src && is < src->n; is++)
+        if (src->shot[is] == ishot && src->comp[is] == 2)
+            IX2(w->vz, src->z[is], src->x[is], g->nxt) += src_signal[(size_t)is * g->nt + it];
+}
+
+/* CPML strips touching a cell, in the order the forward applies them.
+ * kind 0: stress pass (x: ix <= ppad, z: iz <= ppad); kind 1: velocity pass (<). */
+typedef struct {
+    int n, p[2];
+} strips;
+
+static strips x_strips(const orc_grid* g, int ix, int kind) {
+    strips s = {0, {0, 0}};
+    if (g->npml <= 0) return s;
+    const int pnx = g->nxt - 2 * g->ppad + g->fpad - 1;
+    if (ix >= g->fpad && (kind == 0 ? ix <= g->ppad : ix < g->ppad)) s.p[s.n++] = ix - g->fpad;
+    if (ix >= g->nxt - g->ppad - 1 && ix < g->nxt - g->fpad) s.p[s.n++] = ix - pnx;
+    return s;
+}
+
+static strips z_strips(const orc_grid* g, int iz, int kind) {
+    strips s = {0, {0, 0}};
+    if (g->npml <= 0) return s;
+    if (!g->fsurf && iz >= g->fpad && (kind == 0 ? iz <= g->ppad : iz < g->ppad)) s.p[s.n++] = iz - g->fpad;
+    if (iz >= g->nzt - g->ppad - 1 && iz < g->nzt - g->fpad) s.p[s.n++] = iz - bottom_offset(g);
+    return s;
+}
+
+/* Post-CPML derivative u' as the forward computes it from the memory before the step. */
+static double cpml_apply(double u, strips s, const double* mem, size_t stride, size_t off,
+                         const double* a, const double* b, const double* K) {
+    for (int i = 0; i < s.n; i++) {
+        const int p = s.p[i];
+        const double mn = b[p] * mem[(size_t)p * stride + off] + a[p] * u;
+        u = u / K[p] + mn;
+    }
+    return u;
+}
+
+/* Transpose of the CPML chain: ubar' -> ubar, updating the memory adjoints. */
+static double cpml_transpose(double ub, strips s, double* madj, size_t stride, size_t off,
+                             const double* a, const double* b, const double* K) {
+    for (int i = s.n - 1; i >= 0; i--) {
+        const int p = s.p[i];
+        double* mb = &madj[(size_t)p * stride + off];
+        const double tot = *mb + ub;
+        *mb = b[p] * tot;
+        ub = ub / K[p] + a[p] * tot;
+    }
+    return ub;
+}
+
+/* Scatter the transposes of D- / D+ applied at cell c (stride s) with adjoint gb into fb. */
+static void scatter_dminus(double* fb, size_t c, ptrdiff_t s, int fpad, const double* hd, double gb) {
+    for (int k = 1; k <= fpad; k++) {
+        fb[c + (k - 1) * s] += hd[k] * gb;
+        fb[c - k * s] -= hd[k] * gb;
+    }
+}
+static void scatter_dplus(double* fb, size_t c, ptrdiff_t s, int fpad, const double* hd, double gb) {
+    for (int k = 1; k <= fpad; k++) {
+        fb[c + k * s] += hd[k] * gb;
+        fb[c - (k - 1) * s] -= hd[k] * gb;
+    }
+}
+
+/* One reverse step: aw holds the adjoint of state n+1 on entry (receiver
+ * adjoint sources already added) and of state n on exit.  xn / xn1 are the
+ * forward states n and n+1.  Material sensitivities accumulate into g_lam,
+ * g_mu ([nzt][nxt]) and g_muzx, g_rzp, g_rxp ([nzt-1][nxt-1]). */
+static void adjoint_step(const orc_grid* g, const orc_medium* m, const orc_wave* xn, const orc_wave* xn1,
+                         orc_wave* aw, double* g_lam, double* g_mu, double* g_muzx, double* g_rzp,
+                         double* g_rxp) {
+    const int nxt = g->nxt, nzt = g->nzt, fpad = g->fpad, tp = 2 * (g->npml + 1);
+    const double dt = g->dt;
+    double hx[7], hz[7];
+    for (int k = 1; k <= fpad; k++) { hx[k] = g->hc[k] / g->dx; hz[k] = g->hc[k] / g->dz; }
+    /* velocity pass (forward_kernel_PSV_GPU.cu:946-1023), transposed */
+    for (int iz = fpad; iz < nzt - fpad; iz++)
+        for (int ix = fpad; ix < nxt - fpad; ix++) {
+            const size_t c = (size_t)iz * nxt + ix, ca = (size_t)iz * (nxt - 1) + ix;
+            const strips sx = x_strips(g, ix, 1), sz = z_strips(g, iz, 1);
+            double sxx_x = dplus(xn1->sxx, c, 1, fpad, hx);
+            double szx_x = dminus(xn1->szx, c, 1, fpad, hx);
+            double szx_z = dminus(xn1->szx, c, nxt, fpad, hz);
+            double szz_z = dplus(xn1->szz, c, nxt, fpad, hz);
+            sxx_x = cpml_apply(sxx_x, sx, xn->mem_sxx_x, 1, (size_t)iz * tp, g->a, g->b, g->K);
+            szx_x = cpml_apply(szx_x, sx, xn->mem_szx_x, 1, (size_t)iz * tp, g->a_half, g->b_half, g->K_half);
+            szz_z = cpml_apply(szz_z, sz, xn->mem_szz_z, nxt, ix, g->a, g->b, g->K);
+            szx_z = cpml_apply(szx_z, sz, xn->mem_szx_z, nxt, ix, g->a_half, g->b_half, g->K_half);
+            const double vxb = aw->vx[c], vzb = aw->vz[c];
+            const double rxp = m->rho_xp[ca], rzp = m->rho_zp[ca];
+            g_rxp[ca] += vxb * dt * (sxx_x + szx_z);
+            g_rzp[ca] += vzb * dt * (szx_x + szz_z);
+            const double w1 = dt * rxp * vxb, w2 = dt * rzp * vzb;
+            const double gsxx = cpml_transpose(w1, sx, aw->mem_sxx_x, 1, (size_t)iz * tp, g->a, g->b, g->K);
+            const double gszx_x =
+                cpml_transpose(w2, sx, aw->mem_szx_x, 1, (size_t)iz * tp, g->a_half, g->b_half, g->K_half);
+            const double gszz = cpml_transpose(w2, sz, aw->mem_szz_z, nxt, ix, g->a, g->b, g->K);
+            const double gszx_z = cpml_transpose(w1, sz, aw->mem_szx_z, nxt, ix, g->a_half, g->b_half, g->K_half);
+            scatter_dplus(aw->sxx, c, 1, fpad, hx, gsxx);
+            scatter_dminus(aw->szx, c, 1, fpad, hx, gszx_x);
+            scatter_dminus(aw->szx, c, nxt, fpad, hz, gszx_z);
+            scatter_dplus(aw->szz, c, nxt, fpad, hz, gszz);
+        }
+    /* stress mirror above the free surface (:934-942), transposed */
+    if (g->fsurf)
+        for (int ix = fpad; ix < nxt - fpad; ix++)
+            for (int s = 1; s <= fpad; s++) {
+                IX2(aw->szx, fpad + s, ix, nxt) -= IX2(aw->szx, fpad - s, ix, nxt);
+                IX2(aw->szz, fpad + s, ix, nxt) -= IX2(aw->szz, fpad - s, ix, nxt);
+                IX2(aw->szx, fpad - s, ix, nxt) = 0.0;
+                IX2(aw->szz, fpad - s, ix, nxt) = 0.0;
+            }
+    /* stress pass (:830-931), transposed */
+    for (int iz = fpad; iz < nzt - fpad; iz++)
+        for (int ix = fpad; ix < nxt - fpad; ix++) {
+            const size_t c = (size_t)iz * nxt + ix, ca = (size_t)iz * (nxt - 1) + ix;
+            const strips sx = x_strips(g, ix, 0), sz = z_strips(g, iz, 0);
+            double vx_x = dminus(xn->vx, c, 1, fpad, hx);
+            double vz_x = dplus(xn->vz, c, 1, fpad, hx);
+            double vx_z = dplus(xn->vx, c, nxt, fpad, hz);
+            double vz_z = dminus(xn->vz, c, nxt, fpad, hz);
+            vx_x = cpml_apply(vx_x, sx, xn->mem_vx_x, 1, (size_t)iz * tp, g->a, g->b, g->K);
+            vz_x = cpml_apply(vz_x, sx, xn->mem_vz_x, 1, (size_t)iz * tp, g->a_half, g->b_half, g->K_half);
+            vz_z = cpml_apply(vz_z, sz, xn->mem_vz_z, nxt, ix, g->a, g->b, g->K);
+            vx_z = cpml_apply(vx_z, sz, xn->mem_vx_z, nxt, ix, g->a_half, g->b_half, g->K_half);
+            const double lam = m->lam[c], mu = m->mu[c];
+            const double sxxb = aw->sxx[c], szxb = aw->szx[c], szzb = aw->szz[c];
+            double ax, bx, az, bz;  /* adjoints of vx_x', vz_x', vx_z', vz_z' */
+            if (g->fsurf && iz == fpad) {
+                /* sxx = 4 dt vx_x (lam mu + mu^2) / (lam + 2 mu); szz = szx = 0 */
+                const double den = lam + 2.0 * mu;
+                g_lam[c] += sxxb * vx_x * 4.0 * dt * mu * mu / (den * den);
+                g_mu[c] += sxxb * vx_x * 4.0 * dt * (lam * lam + 2.0 * lam * mu + 2.0 * mu * mu) / (den * den);
+                ax = sxxb * 4.0 * dt * (lam * mu + mu * mu) / den;
+                bx = az = bz = 0.0;
+                aw->sxx[c] = aw->szx[c] = aw->szz[c] = 0.0;
+            } else {
+                const double muzx = m->mu_zx[ca];
+                g_muzx[ca] += szxb * dt * (vz_x + vx_z);
+                g_lam[c] += (sxxb + szzb) * dt * (vx_x + vz_z);
+                g_mu[c] += 2.0 * dt * (sxxb * vx_x + szzb * vz_z);
+                ax = dt * (lam + 2.0 * mu) * sxxb + dt * lam * szzb;
+                bz = dt * lam * sxxb + dt * (lam + 2.0 * mu) * szzb;
+                bx = az = dt * muzx * szxb;
+            }
+            ax = cpml_transpose(ax, sx, aw->mem_vx_x, 1, (size_t)iz * tp, g->a, g->b, g->K);
+            bx = cpml_transpose(bx, sx, aw->mem_vz_x, 1, (size_t)iz * tp, g->a_half, g->b_half, g->K_half);
+            bz = cpml_transpose(bz, sz, aw->mem_vz_z, nxt, ix, g->a, g->b, g->K);
+            az = cpml_transpose(az, sz, aw->mem_vx_z, nxt, ix, g->a_half, g->b_half, g->K_half);
+            scatter_dminus(aw->vx, c, 1, fpad, hx, ax);
+            scatter_dplus(aw->vz, c, 1, fpad, hx, bx);
+            scatter_dplus(aw->vx, c, nxt, fpad, hz, az);
+            scatter_dminus(aw->vz, c, nxt, fpad, hz, bz);
+        }
+}
+
+int orc_exact_gradient(int ishot, const orc_grid* g, const double* lam, const double* mu, const double* rho,
+                       const orc_seis* src, const double* src_signal, const orc_seis* rec, const double* obs,
+                       double* misfit, double* grad_lam, double* grad_mu, double* grad_rho) {
+    int rc = check_grid(g);
+    if (rc) return rc;
+    const int nt = g->nt, nzt = g->nzt, nxt = g->nxt;
+    const double dt = g->dt;
+    const st_sizes ss = state_sizes(g);
+    const size_t na = (size_t)(nzt - 1) * (nxt - 1);
+    int K = 1;
+    while ((long long)K * K < nt) K++;
+    const int nck = (nt + K - 1) / K;
+    double* mzx = (double*)calloc(3 * na, sizeof(double));
+    double* chk = (double*)calloc((size_t)nck * ss.total, sizeof(double));
+    double* seg = (double*)calloc((size_t)(K + 1) * ss.total, sizeof(double));
+    double* adj = (double*)calloc(ss.total, sizeof(double));
+    double* we = (double*)calloc(ss.n, sizeof(double));
+    double* gavg = (double*)calloc(3 * na, sizeof(double));
+    double* recs = (double*)calloc((size_t)(rec ? rec->n : 0) * nt + 1, sizeof(double));
+    if (!mzx || !chk || !seg || !adj || !we || !gavg || !recs) {
+        free(mzx); free(chk); free(seg); free(adj); free(we); free(gavg); free(recs);
+        return -4;
+    }
+    orc_average(nzt, nxt, lam, mu, rho, mzx, mzx + na, mzx + 2 * na);
+    orc_medium med = {lam, mu, mzx, mzx + na, mzx + 2 * na};
+    double *g_muzx = gavg, *g_rzp = gavg + na, *g_rxp = gavg + 2 * na;
+    memset(grad_lam, 0, ss.n * sizeof(double));
+    memset(grad_mu, 0, ss.n * sizeof(double));
+    memset(grad_rho, 0, ss.n * sizeof(double));
+    /* forward sweep: checkpoints every K steps, records kept */
+    orc_wave w;
+    wave_view(g, seg, we, &w);
+    double J = 0.0;
+    for (int it = 0; it < nt; it++) {
+        if (it % K == 0) memcpy(chk + (size_t)(it / K) * ss.total, seg, ss.total * sizeof(double));
+        fwd_step(g, &med, &w, it, ishot, src, src_signal);
+        for (int ir = 0; rec && ir < rec->n; ir++)
+            if (rec->shot[ir] == ishot && rec->comp[ir] == 2) {
+                const double v = IX2(w.vz, rec->z[ir], rec->x[ir], nxt);
+                recs[(size_t)ir * nt + it] = v;
+                const double d = v - obs[(size_t)ir * nt + it];
+                J += 0.5 * dt * d * d;
+            }
+    }
+    /* reverse sweep, segment by segment */
+    orc_wave aw;
+    wave_view(g, adj, we, &aw);
+    for (int j = nck - 1; j >= 0; j--) {
+        const int k0 = j * K, k1 = k0 + K < nt ? k0 + K : nt;
+        memcpy(seg, chk + (size_t)j * ss.total, ss.total * sizeof(double));
+        for (int it = k0; it < k1; it++) {
+            double* nxtst = seg + (size_t)(it - k0 + 1) * ss.total;
+            memcpy(nxtst, nxtst - ss.total, ss.total * sizeof(double));
+            orc_wave ws;
+            wave_view(g, nxtst, we, &ws);
+            fwd_step(g, &med, &ws, it, ishot, src, src_signal);
+        }
+        for (int it = k1 - 1; it >= k0; it--) {
+            for (int ir = 0; rec && ir < rec->n; ir++)
+                if (rec->shot[ir] == ishot && rec->comp[ir] == 2)
+                    IX2(aw.vz, rec->z[ir], rec->x[ir], nxt) +=
+                        dt * (recs[(size_t)ir * nt + it] - obs[(size_t)ir * nt + it]);
+            orc_wave xn, xn1;
+            wave_view(g, seg + (size_t)(it - k0) * ss.total, we, &xn);
+            wave_view(g, seg + (size_t)(it - k0 + 1) * ss.total, we, &xn1);
+            adjoint_step(g, &med, &xn, &xn1, &aw, grad_lam, grad_mu, g_muzx, g_rzp, g_rxp);
+        }
+    }
+    /* staggered averages (fd_medium.cu:128-159) -> raw mu and rho */
+    for (int iz = 0; iz < nzt - 1; iz++)
+        for (int ix = 0; ix < nxt - 1; ix++) {
+            const size_t a = (size_t)iz * (nxt - 1) + ix;
+            const double m00 = IX2(mu, iz, ix, nxt), m01 = IX2(mu, iz, ix + 1, nxt);
+            const double m10 = IX2(mu, iz + 1, ix, nxt), m11 = IX2(mu, iz + 1, ix + 1, nxt);
+            if (m00 != 0.0 && m01 != 0.0 && m10 != 0.0 && m11 != 0.0) {
+                const double h = mzx[a], q = g_muzx[a] * h * h / 4.0;
+                IX2(grad_mu, iz, ix, nxt) += q / (m00 * m00);
+                IX2(grad_mu, iz, ix + 1, nxt) += q / (m01 * m01);
+                IX2(grad_mu, iz + 1, ix, nxt) += q / (m10 * m10);
+                IX2(grad_mu, iz + 1, ix + 1, nxt) += q / (m11 * m11);
+            }
+            const double r00 = IX2(rho, iz, ix, nxt), r10 = IX2(rho, iz + 1, ix, nxt);
+            const double r01 = IX2(rho, iz, ix + 1, nxt);
+            const int zguard = (r00 < 1e-4 && r10 < 1e-4) || (r00 < 1e-4 && r01 < 1e-4);
+            if (!zguard) {
+                const double rz = mzx[na + a], dz = -0.5 * rz * rz * g_rzp[a];
+                IX2(grad_rho, iz, ix, nxt) += dz;
+                IX2(grad_rho, iz + 1, ix, nxt) += dz;
+            }
+            const double rx = mzx[2 * na + a], dx = -0.5 * rx * rx * g_rxp[a];
+            IX2(grad_rho, iz, ix, nxt) += dx;
+            IX2(grad_rho, iz, ix + 1, nxt) += dx;
+        }
+    if (misfit) *misfit = J;
+    free(mzx); free(chk); free(seg); free(adj); free(we); free(gavg); free(recs);
+    return 0;
+}

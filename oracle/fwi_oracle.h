@@ -129,6 +129,16 @@ void orc_grad_update(double* mat, double* mat_new, const double* grad, int pitch
 /* fwi_step_length_estimation.cu:226-271 and solvelin.cu:6-42 (float temporaries kept). */
 double orc_calc_opt_step(const double* L2, const double* sl);
 
+/* Exact discrete adjoint of orc_forward's time stepping (no reference
+ * counterpart): dJ/dlam, dJ/dmu, dJ/drho on the padded grid [nzt][nxt] of
+ * J = sum_it sum_r 0.5 dt (rec_r(it) - obs_r(it))^2 over the receivers of
+ * `ishot` (obs is [nrec][nt] in receiver order), with lam, mu, rho the raw
+ * [nzt][nxt] models (the staggered averages are differentiated too).
+ * Returns 0, a check_grid code, or -4 when out of memory. */
+int orc_exact_gradient(int ishot, const orc_grid* g, const double* lam, const double* mu, const double* rho,
+                       const orc_seis* src, const double* src_signal, const orc_seis* rec, const double* obs,
+                       double* misfit, double* grad_lam, double* grad_mu, double* grad_rho);
+
 #ifdef __cplusplus
 }
 #endif

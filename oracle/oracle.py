@@ -78,6 +78,8 @@ def lib():
         L.orc_grad_update.restype = None
         L.orc_calc_opt_step.argtypes = [dp, dp]
         L.orc_calc_opt_step.restype = C.c_double
+        L.orc_exact_gradient.argtypes = [C.c_int, C.POINTER(Grid), dp, dp, dp, C.POINTER(Seis), dp,
+                                         C.POINTER(Seis), dp, dp, dp, dp, dp]
         _lib = L
     return _lib
 
@@ -239,6 +241,35 @@ def gradient(p, obs, shot=0, lam=None, mu=None, rho=None):
     J, res, _ = residual(fw["rec"], obs, p.dt, rows)
     ad = adjoint(p, shot, res, fw["store"], lam, mu, rho)
     return J, (ad["grad_lam"], ad["grad_mu"], ad["grad_rho"]), fw, ad
+
+
+def misfit(p, obs, shot=0, lam=None, mu=None, rho=None):
+    """J = sum 0.5 dt (rec - obs)^2 over the receivers of `shot`, in FP64."""
+    fw = forward(p, shot, False, lam, mu, rho)
+    rows = shot_rows(p, shot)
+    d = fw["rec"][rows] - np.asarray(obs, np.float64)[rows]
+    return float(0.5 * p.dt * np.sum(d * d))
+
+
+def exact_gradient(p, obs, shot=0, lam=None, mu=None, rho=None):
+    """orc_exact_gradient: the discrete adjoint of the oracle's own time
+    stepping.  Returns (J, grad_lam, grad_mu, grad_rho), gradients [nzt][nxt]
+    with respect to the raw (unaveraged) models."""
+    ctx = _Ctx(p, lam, mu, rho)
+    lam = ctx.mat[0]
+    mu = ctx.mat[1]
+    rho = np.ascontiguousarray(p.rho if rho is None else rho, np.float64)
+    src, keep1 = ctx.seis(p.src_x, p.src_z, p.src_comp, p.src_shot)
+    rec, keep2 = ctx.seis(p.rec_x, p.rec_z, p.rec_comp, p.rec_shot)
+    sig = np.ascontiguousarray(p.src_signal, np.float64) if p.nsrc else np.zeros((1, p.nt))
+    ob = np.ascontiguousarray(obs, np.float64) if p.nrec else np.zeros((1, p.nt))
+    g = [np.zeros((p.nzt, p.nxt)) for _ in range(3)]
+    J = C.c_double()
+    rc = lib().orc_exact_gradient(shot, C.byref(ctx.g), _d(lam), _d(mu), _d(rho), C.byref(src), _d(sig),
+                                  C.byref(rec), _d(ob), C.byref(J), *[_d(x) for x in g])
+    if rc != 0:
+        raise ValueError(f"orc_exact_gradient failed ({rc})")
+    return J.value, g[0], g[1], g[2]
 
 
 def calc_opt_step(L2, sl):
