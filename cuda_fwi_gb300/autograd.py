@@ -6,9 +6,10 @@ differentiable function of lam, mu, rho.
 
 forward returns sum over shots of J_s = sum 0.5 dt (syn - obs)^2 (the
 reference's calculate_l2_adjoint_sources, CUDA_week2/fd_wave_model.cu:972-1002);
-backward returns the gradient the engine computes with the reference's
-correlation formula (adjoint_kernel_PSV_GPU.cu:830-863), placed on the FWI
-window cells of the padded grid (zero elsewhere).  The forward and the
+backward returns the gradient the engine computes -- the reference's
+correlation formula (adjoint_kernel_PSV_GPU.cu:830-863) by default, or the
+exact discrete adjoint after engine.set_gradient_mode("exact") -- placed on
+the FWI window cells of the padded grid (zero elsewhere).  The forward and the
 adjoint run together on the GPU in one fwi_psv_gradient call; backward only
 scales the stored gradient.
 

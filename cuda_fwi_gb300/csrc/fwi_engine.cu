@@ -25,6 +25,7 @@
 
 #include "../../include/fwi_psv.h"
 #include "fwi_host.h"
+#include "fwi_exact.cuh"
 #include "fwi_kernels.cuh"
 
 namespace fwi {
@@ -157,6 +158,48 @@ static KernelSet kernels_for(int fp, int map) {
     return map ? kernels_for_map<1>(fp) : kernels_for_map<0>(fp);
 }
 
+// Exact discrete adjoint (fwi_exact.cuh): four cell-parallel kernels per
+// reverse step plus the final chain rule onto lam, mu, rho.
+constexpr int kExactThreads = 256;
+using ExactStepFn = void (*)(dim3, cudaStream_t, const ItemDesc*, const ExactDesc*, int, int, long long);
+struct ExactSet {
+    ExactStepFn vel_local, vel_stencil, str_local, str_stencil;
+};
+template <int FP>
+static void x_vel_local(dim3 g, cudaStream_t s, const ItemDesc* it, const ExactDesc* ex, int nb, int step,
+                        long long cells) {
+    vel_adj_local<FP><<<g, kExactThreads, 0, s>>>(it, ex, nb, step, cells);
+}
+template <int FP>
+static void x_vel_stencil(dim3 g, cudaStream_t s, const ItemDesc* it, const ExactDesc* ex, int nb, int,
+                          long long cells) {
+    vel_adj_stencil<FP><<<g, kExactThreads, 0, s>>>(it, ex, nb, cells);
+}
+template <int FP>
+static void x_str_local(dim3 g, cudaStream_t s, const ItemDesc* it, const ExactDesc* ex, int nb, int,
+                        long long cells) {
+    str_adj_local<FP><<<g, kExactThreads, 0, s>>>(it, ex, nb, cells);
+}
+template <int FP>
+static void x_str_stencil(dim3 g, cudaStream_t s, const ItemDesc* it, const ExactDesc* ex, int nb, int,
+                          long long cells) {
+    str_adj_stencil<FP><<<g, kExactThreads, 0, s>>>(it, ex, nb, cells);
+}
+template <int FP>
+static ExactSet exact_set() {
+    return {x_vel_local<FP>, x_vel_stencil<FP>, x_str_local<FP>, x_str_stencil<FP>};
+}
+static ExactSet exact_for(int fp) {
+    switch (fp) {
+        case 1: return exact_set<1>();
+        case 2: return exact_set<2>();
+        case 3: return exact_set<3>();
+        case 4: return exact_set<4>();
+        case 5: return exact_set<5>();
+        default: return exact_set<6>();
+    }
+}
+
 // ---------------------------------------------------------------------------
 // device buffer
 // ---------------------------------------------------------------------------
@@ -257,6 +300,10 @@ struct Engine {
     DBuf d_fwd, d_adj, d_ws, d_wr, d_ux, d_uz, d_grad, d_gsum, d_store, d_snap;
     DBuf d_evcol_f, d_ev_f, d_evcol_a, d_ev_a, d_rec, d_resid, d_rowmis, d_blow;
     DBuf d_items_f, d_items_a;
+    // exact discrete adjoint: forward state n+1, derivative adjoints + sensitivities, descriptors
+    DBuf d_nxt, d_exact, d_exd, d_items_n;
+    ExactSet xs{};
+    bool zero_mu = false;  // some interior cell has mu == 0 (exact mode unsupported)
     HBuf h_stage, h_rec, h_grad;
     DBuf d_err;  // kernel error flags (bounded waits that timed out)
     bool obs_valid = false;
@@ -334,6 +381,7 @@ struct Engine {
         CUDA_TRY(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
         own_stream = true;
         ks = kernels_for(fpad, kmap);
+        xs = exact_for(fpad);
         CUDA_TRY(cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, device));
         FWI_TRY(d_err.ensure(16));
         CUDA_TRY(cudaMemset(d_err.p, 0, 16));
@@ -350,6 +398,12 @@ struct Engine {
         nf = (size_t)nfz * nfx;
     }
 
+    // The exact adjoint always runs the checkpointed schedule, one time step per unit.
+    bool exact() const { return grad_mode == FWI_GRAD_EXACT; }
+    bool ckpt_mode() const { return strategy == FWI_STORE_BINOMIAL || exact(); }
+    int unit() const { return exact() ? 1 : fwi_dt; }
+    int nunits() const { return exact() ? nt : nft; }
+
     void invalidate_batch() {
         drop_graphs();
         for (auto& kv : tilesets) kv.second->ntiles = 0;
@@ -363,6 +417,9 @@ struct Engine {
         if (!lam || !mu || !mu_zx || !rho_zp || !rho_xp) return fail(FWI_ERR_INVALID, "null material array");
         FWI_TRY(bind());
         std::vector<float> h(5 * field, 0.f);
+        zero_mu = false;
+        for (int iz = fpad; iz < nzt - fpad; iz++)
+            for (int ix = fpad; ix < nxt - fpad; ix++) zero_mu |= mu[(size_t)iz * nxt + ix] == 0.0;
         float* L = h.data();
         float* M2 = L + field;
         float* MZ = M2 + field;
@@ -466,8 +523,10 @@ struct Engine {
         b += 2 * (size_t)nb * state * f;        // fwd + adj state
         b += 4 * (size_t)nb * field * f;        // ws, wr, ux, uz
         b += 3 * (size_t)nb * nf * f + 6 * nf * f;  // grads, sum, accumulator
-        if (strat == FWI_STORE_FULL) b += (size_t)nb * nft * 5 * nf * f;
-        if (strat == FWI_STORE_BINOMIAL) b += (size_t)nslots * nb * state * f;
+        const bool ck = strat == FWI_STORE_BINOMIAL || (strat >= 0 && exact());
+        if (strat == FWI_STORE_FULL && !ck) b += (size_t)nb * nft * 5 * nf * f;
+        if (ck) b += (size_t)nslots * nb * state * f;
+        if (exact()) b += (size_t)nb * (state + 9 * field) * f;  // state n+1, tmp + acc
         return b;
     }
 
@@ -517,7 +576,7 @@ struct Engine {
 
     int slots_for(int nb, bool keep, int* out) {
         *out = 0;
-        if (!(keep && strategy == FWI_STORE_BINOMIAL)) return FWI_OK;
+        if (!(keep && ckpt_mode())) return FWI_OK;
         size_t bud = budget;
         if (bud == 0) {
             size_t fr = 0, tot = 0;
@@ -530,14 +589,14 @@ struct Engine {
         long long fit = bud > base ? (long long)((bud - base) / per_slot) : 0;
         int want = 0;
         if (snapshots_req > 0) {
-            if (fit < std::min(snapshots_req, nft - 1))
+            if (fit < std::min(snapshots_req, nunits() - 1))
                 return fail(FWI_ERR_NOMEM, "budget too small for " + std::to_string(snapshots_req) +
                                                " checkpoints per shot");
             want = snapshots_req;
         } else {
-            want = (int)std::min<long long>(fit, nft - 1);
+            want = (int)std::min<long long>(fit, nunits() - 1);
         }
-        *out = std::max(0, std::min(want, nft - 1));
+        *out = std::max(0, std::min(want, nunits() - 1));
         return FWI_OK;
     }
 
@@ -568,9 +627,14 @@ struct Engine {
         FWI_TRY(grow(d_grad, (size_t)cap * 3 * nf * 4));
         FWI_TRY(grow(d_gsum, (size_t)3 * nf * 4));
         FWI_TRY(grow(d_gacc, (size_t)3 * nf * 4));
-        if (keep && strategy == FWI_STORE_FULL) FWI_TRY(grow(d_store, (size_t)cap * nft * 5 * nf * 4));
-        if (keep && strategy == FWI_STORE_BINOMIAL && want_slots > 0)
-            FWI_TRY(grow(d_snap, (size_t)want_slots * cap * state * 4));
+        if (keep && !ckpt_mode()) FWI_TRY(grow(d_store, (size_t)cap * nft * 5 * nf * 4));
+        if (keep && ckpt_mode() && want_slots > 0) FWI_TRY(grow(d_snap, (size_t)want_slots * cap * state * 4));
+        if (exact()) {
+            FWI_TRY(grow(d_nxt, (size_t)cap * state * 4));
+            FWI_TRY(grow(d_exact, (size_t)cap * 9 * field * 4));
+            FWI_TRY(grow(d_exd, (size_t)cap * sizeof(ExactDesc)));
+            FWI_TRY(grow(d_items_n, (size_t)cap * sizeof(ItemDesc)));
+        }
         rows_cap = std::max(rows_cap, std::max<size_t>(1, nrows));
         FWI_TRY(grow(d_rec, rows_cap * nt * 4));
         FWI_TRY(grow(d_resid, rows_cap * nt * 4));
@@ -636,22 +700,38 @@ struct Engine {
             CUDA_TRY(cudaMemcpyAsync(d_ev_a.p, eva.data(), eva.size() * 8, cudaMemcpyHostToDevice, stream));
         if (nrows)
             CUDA_TRY(cudaMemcpyAsync(d_rowrec.p, rows.data(), nrows * 4, cudaMemcpyHostToDevice, stream));
-        std::vector<ItemDesc> itf(B), ita(B);
+        std::vector<ItemDesc> itf(B), ita(B), itn(B);
+        std::vector<ExactDesc> exd(B);
         for (int b = 0; b < B; b++) {
             fill_item(itf[b], b, false);
             fill_item(ita[b], b, true);
+            if (exact()) {
+                fill_item(itn[b], b, false, d_nxt.as<float>());
+                ExactDesc& x = exd[b];
+                x.tmp = d_exact.as<float>() + (size_t)b * 9 * field;
+                x.acc = x.tmp + 4 * field;
+                x.next = d_nxt.as<float>() + (size_t)b * state;
+                x.src_col = itf[b].ev_col;
+                x.src_ev = itf[b].ev;
+                x.src_sig = d_srcsig.as<float>();
+                x.field = (long long)field;
+            }
         }
         CUDA_TRY(cudaMemcpyAsync(d_items_f.p, itf.data(), B * sizeof(ItemDesc), cudaMemcpyHostToDevice, stream));
         CUDA_TRY(cudaMemcpyAsync(d_items_a.p, ita.data(), B * sizeof(ItemDesc), cudaMemcpyHostToDevice, stream));
+        if (exact()) {
+            CUDA_TRY(cudaMemcpyAsync(d_items_n.p, itn.data(), B * sizeof(ItemDesc), cudaMemcpyHostToDevice, stream));
+            CUDA_TRY(cudaMemcpyAsync(d_exd.p, exd.data(), B * sizeof(ExactDesc), cudaMemcpyHostToDevice, stream));
+        }
         FWI_TRY(tiles_for(B));
         CUDA_TRY(cudaStreamSynchronize(stream));
-        if (keep && strategy == FWI_STORE_BINOMIAL) plan = plan_binomial(nft, slots, &plan_cost);
+        if (keep && ckpt_mode()) plan = plan_binomial(nunits(), slots, &plan_cost);
         return FWI_OK;
     }
     std::string shape_key() const {
         return "|B" + std::to_string(B) + "|r" + std::to_string(rows.size()) + "|s" +
                std::to_string(slots) + "|st" + std::to_string(strategy) + "|t" + std::to_string(ntiles) +
-               "|g" + std::to_string(grad_on ? 1 : 0);
+               "|g" + std::to_string(grad_on ? 1 : 0) + "|m" + std::to_string(grad_mode);
     }
 
     // FP64 host observed data -> resident FP32 rows [nrec][nt] for the given receivers.
@@ -682,11 +762,11 @@ struct Engine {
     size_t allocated_bytes() const {
         size_t t = d_fwd.bytes + d_adj.bytes + d_ws.bytes + d_wr.bytes + d_ux.bytes + d_uz.bytes +
                    d_grad.bytes + d_gsum.bytes + d_gacc.bytes + d_store.bytes + d_snap.bytes +
-                   d_rec.bytes + d_obsf.bytes + d_resid.bytes;
+                   d_rec.bytes + d_obsf.bytes + d_resid.bytes + d_nxt.bytes + d_exact.bytes;
         return t;
     }
 
-    void fill_item(ItemDesc& d, int b, bool adj) {
+    void fill_item(ItemDesc& d, int b, bool adj, float* state_base = nullptr) {
         std::memset(&d, 0, sizeof d);
         d.nzt = nzt; d.nxt = nxt; d.pitch = pitch; d.fpad = fpad;
         d.ppad = ppad; d.npml = npml; d.tp = tp; d.pnx = pnx;
@@ -703,7 +783,7 @@ struct Engine {
         d.cpml = d_cpml.as<float>();
         const float* m = d_mat.as<float>();
         d.L = m; d.M2 = m + field; d.MZX = m + 2 * field; d.BX = m + 3 * field; d.BZ = m + 4 * field;
-        float* st = (adj ? d_adj.as<float>() : d_fwd.as<float>()) + (size_t)b * state;
+        float* st = (state_base ? state_base : adj ? d_adj.as<float>() : d_fwd.as<float>()) + (size_t)b * state;
         d.vx = st + F_VX * field; d.vz = st + F_VZ * field; d.sxx = st + F_SXX * field;
         d.szx = st + F_SZX * field; d.szz = st + F_SZZ * field;
         float* cp = st + 5 * field;
@@ -722,7 +802,7 @@ struct Engine {
             d.glam = d_grad.as<float>() + (size_t)b * 3 * nf;
             d.gmu = d.glam + nf;
             d.grho = d.gmu + nf;
-            if (strategy == FWI_STORE_BINOMIAL) {
+            if (ckpt_mode()) {
                 d.fwd_kind = 1;
                 d.fwd = d_fwd.as<float>() + (size_t)b * state;
                 d.fwd_fs = (long long)field;
@@ -769,6 +849,26 @@ struct Engine {
             unsigned sf = (grad_on && it % fwi_dt == 0) ? FL_GRAD : 0u;
             step(true, it, sf, FL_INJECT | FL_WE);
         }
+    }
+    // One reverse step of the exact discrete adjoint at time step n: the
+    // working forward state (d_fwd) holds state n; state n+1 is made from it
+    // in d_nxt by one more forward step, then the four transposed passes run.
+    int exact_step(int n) {
+        CUDA_TRY(cudaMemcpyAsync(d_nxt.p, d_fwd.p, (size_t)B * state * 4, cudaMemcpyDeviceToDevice, stream));
+        const ItemDesc* itn = d_items_n.as<ItemDesc>();
+        int* err = d_err.as<int>();
+        ks.stress_f(dim3(grid_sf), stream, itn, d_tiles_p, ntiles, n, 0u, err);
+        ks.velocity(dim3(grid_v), stream, itn, d_tiles_p, ntiles, n, FL_INJECT, err);
+        const long long cells = (long long)(nzt - 2 * fpad) * (nxt - 2 * fpad);
+        const dim3 g((unsigned)((cells + kExactThreads - 1) / kExactThreads), (unsigned)B);
+        const ItemDesc* ia = d_items_a.as<ItemDesc>();
+        const ExactDesc* ex = d_exd.as<ExactDesc>();
+        xs.vel_local(g, stream, ia, ex, B, n, cells);
+        xs.vel_stencil(g, stream, ia, ex, B, n, cells);
+        xs.str_local(g, stream, ia, ex, B, n, cells);
+        xs.str_stencil(g, stream, ia, ex, B, n, cells);
+        launches_now += 6;
+        return FWI_OK;
     }
     int state_copy(float* dst, const float* src) {
         CUDA_TRY(cudaMemcpyAsync(dst, src, (size_t)B * state * 4, cudaMemcpyDeviceToDevice, stream));
@@ -827,8 +927,8 @@ struct Engine {
         CUDA_TRY(cudaEventCreate(&e1));
         launches_now = 0;
         CUDA_TRY(cudaEventRecord(e0, stream));
-        const bool store = keep && strategy == FWI_STORE_FULL;
-        const bool ckpt = keep && strategy == FWI_STORE_BINOMIAL;
+        const bool store = keep && !ckpt_mode();
+        const bool ckpt = keep && ckpt_mode();
         // checkpoint positions of the first sweep: the SAVE actions before the first ADJOINT
         std::vector<std::pair<int, int>> saves;  // (state, slot)
         if (ckpt)
@@ -843,7 +943,7 @@ struct Engine {
             CUDA_TRY(cudaMemsetAsync(d_ws.p, 0, (size_t)B * field * 4, stream));
             int t = 0;
             for (auto& sv : saves) {
-                const int tstate = sv.first * fwi_dt;
+                const int tstate = sv.first * unit();
                 forward_steps(t, tstate, true, false);
                 t = tstate;
                 FWI_TRY(state_copy(snap(sv.second), d_fwd.as<float>()));
@@ -911,7 +1011,7 @@ struct Engine {
         int* er = d_err.as<int>();
         const ItemDesc* itf = d_items_f.as<ItemDesc>();
         const ItemDesc* ita = d_items_a.as<ItemDesc>();
-        const bool have_adj_src = strategy != FWI_STORE_BINOMIAL ? d_store.p != nullptr : true;
+        const bool have_adj_src = ckpt_mode() ? true : d_store.p != nullptr;
         for (int k = 0; k < 4; k++) {
             const bool adj = k >= 2;
             if (adj && !have_adj_src) { ms[k] = 0.0; continue; }
@@ -943,22 +1043,25 @@ struct Engine {
         FWI_TRY(bind());
         if (!fwd_kept) return fail(FWI_ERR_NOFORWARD, "backward needs a forward(keep=1)");
         if (!have_resid) return fail(FWI_ERR_STATE, "backward needs observed data (forward obs) or a loaded residual");
-        if (bwd_done && strategy == FWI_STORE_BINOMIAL)
+        if (bwd_done && ckpt_mode())
             return fail(FWI_ERR_STATE, "the checkpointed forward was consumed by the previous backward");
+        if (exact() && zero_mu)
+            return fail(FWI_ERR_UNSUPPORTED, "the exact adjoint needs mu > 0 on every interior cell");
         cudaEvent_t e0, e1;
         CUDA_TRY(cudaEventCreate(&e0));
         CUDA_TRY(cudaEventCreate(&e1));
         launches_now = 0;
         long long recompute = 0;
         CUDA_TRY(cudaEventRecord(e0, stream));
-        const std::string key = std::string(strategy == FWI_STORE_BINOMIAL ? "bwdC" : "bwdS") + shape_key();
+        const std::string key = std::string(ckpt_mode() ? "bwdC" : "bwdS") + shape_key();
         FWI_TRY(run_phase(key, [&]() -> int {
             CUDA_TRY(cudaMemsetAsync(d_adj.p, 0, (size_t)B * state * 4, stream));
             CUDA_TRY(cudaMemsetAsync(d_wr.p, 0, (size_t)B * field * 4, stream));
             CUDA_TRY(cudaMemsetAsync(d_ux.p, 0, (size_t)B * field * 4, stream));
             CUDA_TRY(cudaMemsetAsync(d_uz.p, 0, (size_t)B * field * 4, stream));
             CUDA_TRY(cudaMemsetAsync(d_grad.p, 0, (size_t)B * 3 * nf * 4, stream));
-            if (strategy != FWI_STORE_BINOMIAL) {
+            if (exact()) CUDA_TRY(cudaMemsetAsync(d_exact.p, 0, (size_t)B * 9 * field * 4, stream));
+            if (!ckpt_mode()) {
                 adjoint_steps(0, nt);
                 return FWI_OK;
             }
@@ -973,13 +1076,14 @@ struct Engine {
             // working buffer: state of the last prefix checkpoint, advanced to nft-1
             if (last_slot >= 0) FWI_TRY(state_copy(d_fwd.as<float>(), snap(last_slot)));
             else CUDA_TRY(cudaMemsetAsync(d_fwd.p, 0, (size_t)B * state * 4, stream));
-            forward_steps(last_state * fwi_dt, (nft - 1) * fwi_dt, false, false);
-            recompute += (nft - 1) - last_state;
+            const int u = unit();
+            forward_steps(last_state * u, (nunits() - 1) * u, false, false);
+            recompute += (nunits() - 1) - last_state;
             for (; k < plan.size(); k++) {
                 const Action& a = plan[k];
                 switch (a.kind) {
                     case Action::ADVANCE:
-                        forward_steps(a.a * fwi_dt, a.b * fwi_dt, false, false);
+                        forward_steps(a.a * u, a.b * u, false, false);
                         recompute += a.b - a.a;
                         break;
                     case Action::SAVE:
@@ -990,11 +1094,21 @@ struct Engine {
                         else FWI_TRY(state_copy(d_fwd.as<float>(), snap(a.a)));
                         break;
                     case Action::ADJOINT: {
+                        if (exact()) {
+                            FWI_TRY(exact_step(a.a));
+                            recompute += 1;  // state n+1 of the reverse step
+                            break;
+                        }
                         const int t0 = a.a * fwi_dt, t1 = std::min(nt, (a.a + 1) * fwi_dt);
                         adjoint_steps(t0, t1);
                         break;
                     }
                 }
+            }
+            if (exact()) {
+                const dim3 g((unsigned)((nf + kExactThreads - 1) / kExactThreads), (unsigned)B);
+                chain_rule<<<g, kExactThreads, 0, stream>>>(d_items_a.as<ItemDesc>(), d_exd.as<ExactDesc>(), B);
+                launches_now++;
             }
             return FWI_OK;
         }));
@@ -1025,9 +1139,7 @@ struct Engine {
         stats.last_backward_ms = ms;
         stats.launches = launches_now;
         stats.adjoint_steps = nt;
-        stats.recompute_steps = strategy == FWI_STORE_BINOMIAL
-                                    ? (recompute > 0 ? recompute : plan_cost) * fwi_dt
-                                    : 0;
+        stats.recompute_steps = ckpt_mode() ? (recompute > 0 ? recompute : plan_cost) * unit() : 0;
         for (size_t s = 0; s < ntrip && want; s++)
             for (size_t i = 0; i < nf; i++) {
                 const float* t = g + s * 3 * nf;
@@ -1391,7 +1503,7 @@ int fwi_psv_set_strategy(fwi_psv_engine* h, int strategy, int snapshots, size_t 
 int fwi_psv_set_gradient_mode(fwi_psv_engine* h, int mode) {
     GUARD_ENGINE(h);
     if (mode != FWI_GRAD_REFERENCE && mode != FWI_GRAD_EXACT) return fail(FWI_ERR_INVALID, "unknown mode");
-    if (mode == FWI_GRAD_EXACT) return fail(FWI_ERR_UNSUPPORTED, "exact discrete adjoint not available in this build");
+    if (h->e.grad_mode != mode) h->e.invalidate_batch();
     h->e.grad_mode = mode;
     return FWI_OK;
 }

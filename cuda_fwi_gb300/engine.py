@@ -88,6 +88,13 @@ class Engine:
         s = STRATEGIES[strategy] if isinstance(strategy, str) else int(strategy)
         check(_capi.lib().fwi_psv_set_strategy(self.h, s, snapshots, budget_bytes), "set_strategy")
 
+    def set_gradient_mode(self, mode="reference"):
+        """'reference': the reference's correlation gradient; 'exact': the
+        discrete adjoint of the FP32 time stepping (gradient of the misfit the
+        forward returns, with respect to the raw lam, mu, rho)."""
+        m = {"reference": 0, "exact": 1}[mode] if isinstance(mode, str) else int(mode)
+        check(_capi.lib().fwi_psv_set_gradient_mode(self.h, m), "set_gradient_mode")
+
     def set_exec(self, use_graphs=True, block_x=0, tile_z=0, batch=0):
         check(_capi.lib().fwi_psv_set_exec(self.h, int(use_graphs), block_x, tile_z, batch), "set_exec")
 

@@ -210,18 +210,20 @@ def config1(anomaly: bool = True) -> Problem:
     return p
 
 
-def config2(perturbed: bool = True) -> Problem:
+def config2(perturbed: bool = True, nx: int = 800, nz: int = 400, nt: int = 4000, npml: int = 30,
+            nrec: int = 200, seed: int = 2) -> Problem:
     """800x400, dx=5, dt=0.5ms, nt=4000, order 8, npml 30; 6 flat layers
-    1800->4500 m/s, Vs=Vp/1.73, Gardner density, +-3% smoothed perturbation."""
-    nx, nz = 800, 400
-    p = Problem(nx=nx, nz=nz, nt=4000, dx=5.0, dz=5.0, dt=0.5e-3, fdorder=8, npml=30,
+    1800->4500 m/s, Vs=Vp/1.73, Gardner density, +-3% smoothed perturbation
+    (correlation length 100 m).  The size arguments give the same physics on a
+    smaller grid or a shorter record."""
+    p = Problem(nx=nx, nz=nz, nt=nt, dx=5.0, dz=5.0, dt=0.5e-3, fdorder=8, npml=npml,
                 fpml=15.0, damp_v_pml=4500.0, name="config2").finalize()
     vp = layered(nz, nx, np.linspace(1800.0, 4500.0, 6))
     if perturbed:
-        vp = vp * (1.0 + smooth_perturbation((nz, nx), 100.0 / 5.0, 0.03, seed=2))
+        vp = vp * (1.0 + smooth_perturbation((nz, nx), 100.0 / 5.0, 0.03, seed=seed))
     p.pad_model(vp, vp / 1.73, gardner(vp))
     p.set_sources([nx // 2], [5], [0], 15.0)
-    p.set_receivers(surface_spread(nx, 200), np.full(200, 5), np.zeros(200, np.int32))
+    p.set_receivers(surface_spread(nx, nrec), np.full(nrec, 5), np.zeros(nrec, np.int32))
     return p
 
 

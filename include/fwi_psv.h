@@ -104,7 +104,14 @@ enum {
     FWI_STORE_RANDOM = 2    /* random-boundary wavefield reconstruction (no CPML on the source side) */
 };
 
-/* Gradient formula. */
+/* Gradient formula.
+ * FWI_GRAD_EXACT has no reference counterpart: it is dJ/d(lam, mu, rho) of
+ * J = sum 0.5 dt (syn-obs)^2 for the raw (unaveraged) models, sampled at the
+ * FWI window's grid points (fwi_dt does not apply: every time step enters).
+ * It always runs the checkpointed schedule, one time step per unit (snapshots
+ * and budget as for FWI_STORE_BINOMIAL, whatever the strategy), needs mu > 0
+ * on every interior cell, and its backward returns FWI_ERR_UNSUPPORTED
+ * otherwise. */
 enum {
     FWI_GRAD_REFERENCE = 0, /* the reference's correlation kernel (adjoint_kernel_PSV_GPU.cu:830-863) */
     FWI_GRAD_EXACT = 1      /* discrete adjoint of the FP32 scheme (matches finite differences) */
