@@ -52,6 +52,8 @@ def parse():
     ap.add_argument("--plain-shots", type=int, default=1)
     ap.add_argument("--batch", type=int, default=0, help="shots per launch (0 = engine default)")
     ap.add_argument("--cpu-nt-sample", type=int, default=200)
+    ap.add_argument("--block-x", type=int, default=0,
+                    help="stencil thread mapping (set_exec block_x; 0 = engine default)")
     ap.add_argument("--no-cpu", action="store_true")
     return ap.parse_args()
 
@@ -170,6 +172,21 @@ def run_reference(args, rank):
     print(json.dumps(out), flush=True)
 
 
+def kernel_names(block_x, fp):
+    """The four timed kernels of the thread mapping set_exec(block_x) selects."""
+    if block_x in (0, 256):  # TMA-staged tiles (the engine default)
+        return [f"stress_tma_kernel<{fp}> (forward/recompute stress+CPML, TMA-staged 128x16 tiles)",
+                f"velocity_tma_kernel<{fp}> (forward/recompute velocity+CPML, TMA-staged 128x16 tiles)",
+                f"adjoint_tma_kernel<{fp}> (adjoint stress+CPML+ux/uz+gradient, TMA-staged 128x8 tiles)",
+                f"velocity_tma_kernel<{fp}> (adjoint velocity+CPML+energy, TMA-staged 128x16 tiles)"]
+    amap = 1 if block_x in (32, 64) else 0
+    vmap = {32: 1, 64: 2}.get(block_x, 0)
+    return [f"stress_kernel<{fp},false,{vmap}> (forward/recompute stress+CPML)",
+            f"velocity_kernel<{fp},{vmap}> (forward/recompute velocity+CPML)",
+            f"stress_kernel<{fp},true,{amap}> (adjoint stress+CPML+ux/uz+gradient)",
+            f"velocity_kernel<{fp},{vmap}> (adjoint velocity+CPML+energy)"]
+
+
 def algorithmic_bytes(p, B):
     """Minimal DRAM bytes of one launch over B shots (FP32): per-shot fields
     once, shared materials once per launch, CPML memory of strip cells."""
@@ -222,7 +239,7 @@ def main():
     eng = Engine(syn, device=local)
     eng.set_stream(stream.cuda_stream)
     eng.set_strategy("binomial", snapshots=args.snapshots)
-    eng.set_exec(True, 0, 0, args.batch)
+    eng.set_exec(True, args.block_x, 0, args.batch)
 
     def step_resident():
         # one batch of shot gradients, observed data resident in HBM, summed gradient left on the device
@@ -296,10 +313,7 @@ def main():
     b_sf, b_vf, b_sa, b_va = algorithmic_bytes(syn, sub)
     counts = [syn.nt + recompute, syn.nt + recompute, syn.nt, syn.nt]
     shares = [c * t for c, t in zip(counts, ms)]
-    names = ["stress_kernel<4,false,2> (forward/recompute stress+CPML, float4 cells)",
-             "velocity_kernel<4,2> (forward velocity+CPML+events, float4 cells)",
-             "stress_kernel<4,true,1> (adjoint stress+CPML+ux/uz+gradient, cells)",
-             "velocity_kernel<4,2> (adjoint velocity+CPML+residual, float4 cells)"]
+    names = kernel_names(args.block_x, syn.fpad)
     dom = max(range(4), key=lambda i: shares[i])
     peak, peak_kind = peaks()
     achieved = [b / (t / 1e3) / 1e9 for b, t in zip((b_sf, b_vf, b_sa, b_va), ms)]
@@ -315,7 +329,7 @@ def main():
     plain = None
     if rank == 0 and args.plain_shots > 0:
         pe = Engine(syn, device=local)
-        pe.set_exec(False, 0, 0, 1)
+        pe.set_exec(False, args.block_x, 0, 1)
         pe.set_strategy("binomial", snapshots=args.snapshots)
         pe.gradient([0], obs)
         torch.cuda.synchronize()

@@ -27,6 +27,7 @@
 #include "fwi_host.h"
 #include "fwi_exact.cuh"
 #include "fwi_kernels.cuh"
+#include "fwi_tma.cuh"
 
 namespace fwi {
 
@@ -78,6 +79,35 @@ __global__ void residual_kernel(const float* __restrict__ syn, const float* __re
         row_misfit[r] = sh[0];
         if (sb) atomicOr(blowup, 1);
     }
+}
+
+// Source injection and receiver recording of one batch slot per block, after
+// a velocity pass that did neither (the TMA mapping): the injections of a
+// cell are added in event order by one thread (events are sorted by column,
+// row, injections first), then the receivers read vz
+// (forward_kernel_PSV_GPU.cu:1033-1063 order).
+__global__ void events_kernel(const ItemDesc* __restrict__ items, int it, unsigned flags) {
+    const ItemDesc& D = items[blockIdx.x];
+    const int e0 = D.ev_col[0], e1 = D.ev_col[D.nxt];
+    const int nt = D.nt, P = D.pitch;
+    if (flags & FL_INJECT)
+        for (int e = e0 + (int)threadIdx.x; e < e1; e += blockDim.x) {
+            const int2 v = D.ev[e];
+            const int x = D.ev_x[e];
+            if (v.y < 0) continue;
+            if (e > e0 && D.ev_x[e - 1] == x && D.ev[e - 1].x == v.x) continue;  // not the cell's first
+            float* c = D.vz + (size_t)v.x * P + x;
+            float val = *c;
+            for (int q = e; q < e1 && D.ev_x[q] == x && D.ev[q].x == v.x && D.ev[q].y >= 0; q++)
+                val += D.inj[(size_t)D.ev[q].y * nt + it];
+            *c = val;
+        }
+    __syncthreads();
+    if (flags & FL_RECORD)
+        for (int e = e0 + (int)threadIdx.x; e < e1; e += blockDim.x) {
+            const int2 v = D.ev[e];
+            if (v.y < 0) D.rec[(size_t)(~v.y) * nt + it] = D.vz[(size_t)v.x * P + D.ev_x[e]];
+        }
 }
 
 // sum the per-shot gradient triples: out[i] = sum_b in[b*n + i]
@@ -155,12 +185,102 @@ static KernelSet kernels_for_map(int fp) {
 }
 static KernelSet kernels_for(int fp, int map) {
     if (map == 2 && fp <= 4) return kernels_for_map<2>(fp);
+    // the TMA mapping (3) runs its adjoint stress pass on the scalar cells
     return map ? kernels_for_map<1>(fp) : kernels_for_map<0>(fp);
+}
+
+// TMA-staged forward stress and velocity passes (fwi_tma.cuh).
+using TmaStressFn = void (*)(dim3, cudaStream_t, const StressMaps&, const ItemDesc*, TmaGrid, int, unsigned, int*);
+using TmaVelFn = void (*)(dim3, cudaStream_t, const VelMaps&, const ItemDesc*, TmaGrid, int, unsigned, int*);
+using TmaAdjFn = void (*)(dim3, cudaStream_t, const AdjMaps&, const ItemDesc*, TmaGrid, int, unsigned, int*);
+struct TmaSet {
+    TmaStressFn stress;
+    TmaVelFn velocity;
+    TmaAdjFn adjoint;
+    cudaError_t (*prepare)();  // opt in to the dynamic shared memory
+};
+template <int FP>
+static void t_stress(dim3 g, cudaStream_t s, const StressMaps& m, const ItemDesc* it, TmaGrid tg, int step,
+                     unsigned flags, int* err) {
+    stress_tma_kernel<FP><<<g, kTmaThreads, stress_tma_smem<FP>(), s>>>(m, it, tg, step, flags, err);
+}
+template <int FP>
+static void t_velocity(dim3 g, cudaStream_t s, const VelMaps& m, const ItemDesc* it, TmaGrid tg, int step,
+                       unsigned flags, int* err) {
+    velocity_tma_kernel<FP><<<g, kTmaThreads, velocity_tma_smem<FP>(), s>>>(m, it, tg, step, flags, err);
+}
+template <int FP>
+static void t_adjoint(dim3 g, cudaStream_t s, const AdjMaps& m, const ItemDesc* it, TmaGrid tg, int step,
+                      unsigned flags, int* err) {
+    adjoint_tma_kernel<FP><<<g, kTmaThreads, adjoint_tma_smem<FP>(), s>>>(m, it, tg, step, flags, err);
+}
+template <int FP>
+static cudaError_t t_prepare() {
+    cudaError_t e = cudaFuncSetAttribute(stress_tma_kernel<FP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)stress_tma_smem<FP>());
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(adjoint_tma_kernel<FP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)adjoint_tma_smem<FP>());
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(velocity_tma_kernel<FP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)velocity_tma_smem<FP>());
+}
+template <int FP>
+static TmaSet tma_set() {
+    return {t_stress<FP>, t_velocity<FP>, t_adjoint<FP>, t_prepare<FP>};
+}
+static TmaSet tma_for(int fp) {
+    switch (fp) {
+        case 1: return tma_set<1>();
+        case 2: return tma_set<2>();
+        case 3: return tma_set<3>();
+        case 4: return tma_set<4>();
+        case 5: return tma_set<5>();
+        default: return tma_set<6>();
+    }
+}
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link-time
+// dependency on libcuda).
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+static EncodeTiledFn encode_tiled() {
+    static EncodeTiledFn fn = nullptr;
+    if (!fn) {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(p);
+    }
+    return fn;
+}
+
+// FP32 tensor map of nb slices [nz][nx] (row stride row_bytes, slice stride
+// slice_bytes; nb == 0 makes a 2-D map), box bx x bz (x 1), zero fill outside.
+static int make_map(CUtensorMap* m, const float* base, int nx, int nz, int nb, size_t row_bytes,
+                    size_t slice_bytes, int bx, int bz) {
+    EncodeTiledFn enc = encode_tiled();
+    if (!enc) return fail(FWI_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+    const cuuint64_t dims[3] = {(cuuint64_t)nx, (cuuint64_t)nz, (cuuint64_t)std::max(nb, 1)};
+    const cuuint64_t strides[2] = {(cuuint64_t)row_bytes, (cuuint64_t)slice_bytes};
+    const cuuint32_t box[3] = {(cuuint32_t)bx, (cuuint32_t)bz, 1};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    const cuuint32_t rank = nb > 0 ? 3 : 2;
+    CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, rank, const_cast<float*>(base), dims, strides, box, estr,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS)
+        return fail(FWI_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+    return FWI_OK;
 }
 
 // Exact discrete adjoint (fwi_exact.cuh): four cell-parallel kernels per
 // reverse step plus the final chain rule onto lam, mu, rho.
 constexpr int kExactThreads = 256;
+constexpr int kDefaultMap = 3;  // thread mapping of a new engine (TMA-staged tiles)
 using ExactStepFn = void (*)(dim3, cudaStream_t, const ItemDesc*, const ExactDesc*, int, int, long long);
 struct ExactSet {
     ExactStepFn vel_local, vel_stencil, str_local, str_stencil;
@@ -298,18 +418,25 @@ struct Engine {
     std::vector<int> rows;  // receiver index of each batch row
     std::vector<int> row_slot;
     DBuf d_fwd, d_adj, d_ws, d_wr, d_ux, d_uz, d_grad, d_gsum, d_store, d_snap;
-    DBuf d_evcol_f, d_ev_f, d_evcol_a, d_ev_a, d_rec, d_resid, d_rowmis, d_blow;
+    DBuf d_evcol_f, d_ev_f, d_evcol_a, d_ev_a, d_evx_f, d_evx_a, d_rec, d_resid, d_rowmis, d_blow;
     DBuf d_items_f, d_items_a;
     // exact discrete adjoint: forward state n+1, derivative adjoints + sensitivities, descriptors
     DBuf d_nxt, d_exact, d_exd, d_items_n;
     ExactSet xs{};
+    // TMA mapping: kernels, tensor maps per state buffer (0 fwd, 1 adj, 2 state n+1), tile grid
+    TmaSet tset{};
+    StressMaps smaps[3];
+    VelMaps vmaps[3];
+    AdjMaps amap;
+    TmaGrid tgrid{}, tgrid_a{};
+    int grid_tma = 1, grid_tma_a = 1;
     bool zero_mu = false;  // some interior cell has mu == 0 (exact mode unsupported)
     HBuf h_stage, h_rec, h_grad;
     DBuf d_err;  // kernel error flags (bounded waits that timed out)
     bool obs_valid = false;
     int ntiles = 0, bx = 128, tz = 32;
     KernelSet ks{};
-    int kmap = 2;  // thread mapping of the stencil kernels (0 z-march, 1 cells, 2 vector cells)
+    int kmap = kDefaultMap;  // thread mapping of the stencil kernels (0 z-march, 1 cells, 2 vector cells, 3 TMA tiles)
     int grid_sf = 1, grid_sa = 1, grid_v = 1, num_sms = 1;
     int slots = 0;  // checkpoint slots per shot (binomial)
     bool fwd_kept = false, have_resid = false, bwd_done = false, grad_on = true;
@@ -382,6 +509,8 @@ struct Engine {
         own_stream = true;
         ks = kernels_for(fpad, kmap);
         xs = exact_for(fpad);
+        tset = tma_for(fpad);
+        if (kmap == 3) CUDA_TRY(tset.prepare());
         CUDA_TRY(cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, device));
         FWI_TRY(d_err.ensure(16));
         CUDA_TRY(cudaMemset(d_err.p, 0, 16));
@@ -656,6 +785,7 @@ struct Engine {
         struct Ev { int x, z, kind, idx, code; };
         std::vector<int> colf((size_t)B * (nxt + 1)), cola((size_t)B * (nxt + 1));
         std::vector<int2> evf, eva;
+        std::vector<int> evxf, evxa;
         for (int b = 0; b < B; b++) {
             std::vector<Ev> ef, ea;
             for (int i = 0; i < nsrc; i++)
@@ -674,7 +804,7 @@ struct Engine {
             };
             std::sort(ef.begin(), ef.end(), cmp);
             std::sort(ea.begin(), ea.end(), cmp);
-            auto fill = [&](std::vector<Ev>& ev, std::vector<int>& col, std::vector<int2>& flat) {
+            auto fill = [&](std::vector<Ev>& ev, std::vector<int>& col, std::vector<int2>& flat, std::vector<int>& fx) {
                 const int base = (int)flat.size();
                 int* c = col.data() + (size_t)b * (nxt + 1);
                 size_t k = 0;
@@ -682,16 +812,25 @@ struct Engine {
                     while (k < ev.size() && ev[k].x < x) k++;
                     c[x] = base + (int)k;
                 }
-                for (auto& e : ev) flat.push_back(make_int2(e.z, e.code));
+                for (auto& e : ev) {
+                    flat.push_back(make_int2(e.z, e.code));
+                    fx.push_back(e.x);
+                }
             };
-            fill(ef, colf, evf);
-            fill(ea, cola, eva);
+            fill(ef, colf, evf, evxf);
+            fill(ea, cola, eva, evxa);
         }
         // event tables are reached through the item descriptors only (not captured)
         FWI_TRY(d_evcol_f.ensure(colf.size() * 4));
         FWI_TRY(d_evcol_a.ensure(cola.size() * 4));
         FWI_TRY(d_ev_f.ensure(std::max<size_t>(1, evf.size()) * 8));
         FWI_TRY(d_ev_a.ensure(std::max<size_t>(1, eva.size()) * 8));
+        FWI_TRY(d_evx_f.ensure(std::max<size_t>(1, evxf.size()) * 4));
+        FWI_TRY(d_evx_a.ensure(std::max<size_t>(1, evxa.size()) * 4));
+        if (!evxf.empty())
+            CUDA_TRY(cudaMemcpyAsync(d_evx_f.p, evxf.data(), evxf.size() * 4, cudaMemcpyHostToDevice, stream));
+        if (!evxa.empty())
+            CUDA_TRY(cudaMemcpyAsync(d_evx_a.p, evxa.data(), evxa.size() * 4, cudaMemcpyHostToDevice, stream));
         CUDA_TRY(cudaMemcpyAsync(d_evcol_f.p, colf.data(), colf.size() * 4, cudaMemcpyHostToDevice, stream));
         CUDA_TRY(cudaMemcpyAsync(d_evcol_a.p, cola.data(), cola.size() * 4, cudaMemcpyHostToDevice, stream));
         if (!evf.empty())
@@ -724,10 +863,99 @@ struct Engine {
             CUDA_TRY(cudaMemcpyAsync(d_exd.p, exd.data(), B * sizeof(ExactDesc), cudaMemcpyHostToDevice, stream));
         }
         FWI_TRY(tiles_for(B));
+        if (kmap == 3) FWI_TRY(build_tma_maps());
         CUDA_TRY(cudaStreamSynchronize(stream));
         if (keep && ckpt_mode()) plan = plan_binomial(nunits(), slots, &plan_cost);
         return FWI_OK;
     }
+    // Tensor maps of the TMA passes for the current buffers (addresses are
+    // captured by value in the launches; buffers only grow, and a regrowth
+    // drops every graph, so maps are rebuilt here with each batch layout).
+    int build_tma_maps() {
+        const int FPv = fpad;
+        const int hx = (FPv + 3) / 4 * 4;
+        const int wx = kTmaTX + 2 * hx, wz = kTmaTZ + 2 * FPv;
+        const size_t rb = (size_t)pitch * 4, sb = state * 4;
+        const float* mat = d_mat.as<float>();
+        float* bases[3] = {d_fwd.as<float>(), d_adj.as<float>(), d_nxt.p ? d_nxt.as<float>() : nullptr};
+        float* webase[3] = {d_ws.as<float>(), d_wr.as<float>(), d_ws.as<float>()};
+        for (int w = 0; w < 3; w++) {
+            float* st = bases[w];
+            if (!st) continue;
+            StressMaps& S = smaps[w];
+            FWI_TRY(make_map(&S.vx, st + F_VX * field, nxt, nzt, Bcap, rb, sb, wx, wz));
+            FWI_TRY(make_map(&S.vz, st + F_VZ * field, nxt, nzt, Bcap, rb, sb, wx, wz));
+            FWI_TRY(make_map(&S.L, mat, nxt, nzt, 0, rb, 0, kTmaTX, kTmaTZ));
+            FWI_TRY(make_map(&S.M2, mat + field, nxt, nzt, 0, rb, 0, kTmaTX, kTmaTZ));
+            FWI_TRY(make_map(&S.MZ, mat + 2 * field, nxt, nzt, 0, rb, 0, kTmaTX, kTmaTZ));
+            FWI_TRY(make_map(&S.sxx, st + F_SXX * field, nxt, nzt, Bcap, rb, sb, kTmaTX, kTmaTZ));
+            FWI_TRY(make_map(&S.szx, st + F_SZX * field, nxt, nzt, Bcap, rb, sb, kTmaTX, kTmaTZ));
+            FWI_TRY(make_map(&S.szz, st + F_SZZ * field, nxt, nzt, Bcap, rb, sb, kTmaTX, kTmaTZ));
+            VelMaps& V = vmaps[w];
+            FWI_TRY(make_map(&V.sxx, st + F_SXX * field, nxt, nzt, Bcap, rb, sb, wx, kTmaTZ));
+            FWI_TRY(make_map(&V.szx, st + F_SZX * field, nxt, nzt, Bcap, rb, sb, wx, wz));
+            FWI_TRY(make_map(&V.szz, st + F_SZZ * field, nxt, nzt, Bcap, rb, sb, kTmaTX, wz));
+            FWI_TRY(make_map(&V.BX, mat + 3 * field, nxt, nzt, 0, rb, 0, kTmaTX, kTmaTZ));
+            FWI_TRY(make_map(&V.BZ, mat + 4 * field, nxt, nzt, 0, rb, 0, kTmaTX, kTmaTZ));
+            FWI_TRY(make_map(&V.vx, st + F_VX * field, nxt, nzt, Bcap, rb, sb, kTmaTX, kTmaTZ));
+            FWI_TRY(make_map(&V.vz, st + F_VZ * field, nxt, nzt, Bcap, rb, sb, kTmaTX, kTmaTZ));
+            FWI_TRY(make_map(&V.We, webase[w], nxt, nzt, Bcap, rb, field * 4, kTmaTX, kTmaTZ));
+        }
+        {
+            // adjoint stress pass (128 x 8 tiles): adjoint state, ux/uz, forward state
+            const int wza = kAdjTZ + 2 * FPv;
+            float* a = d_adj.as<float>();
+            float* f = d_fwd.as<float>();
+            const size_t fb = field * 4;
+            AdjMaps& A = amap;
+            FWI_TRY(make_map(&A.vx, a + F_VX * field, nxt, nzt, Bcap, rb, sb, wx, wza));
+            FWI_TRY(make_map(&A.vz, a + F_VZ * field, nxt, nzt, Bcap, rb, sb, wx, wza));
+            FWI_TRY(make_map(&A.L, mat, nxt, nzt, 0, rb, 0, kTmaTX, kAdjTZ));
+            FWI_TRY(make_map(&A.M2, mat + field, nxt, nzt, 0, rb, 0, kTmaTX, kAdjTZ));
+            FWI_TRY(make_map(&A.MZ, mat + 2 * field, nxt, nzt, 0, rb, 0, kTmaTX, kAdjTZ));
+            FWI_TRY(make_map(&A.sxx, a + F_SXX * field, nxt, nzt, Bcap, rb, sb, kTmaTX, kAdjTZ));
+            FWI_TRY(make_map(&A.szx, a + F_SZX * field, nxt, nzt, Bcap, rb, sb, kTmaTX, kAdjTZ));
+            FWI_TRY(make_map(&A.szz, a + F_SZZ * field, nxt, nzt, Bcap, rb, sb, kTmaTX, kAdjTZ));
+            FWI_TRY(make_map(&A.ux, d_ux.as<float>(), nxt, nzt, Bcap, rb, fb, kTmaTX, kAdjTZ));
+            FWI_TRY(make_map(&A.uz, d_uz.as<float>(), nxt, nzt, Bcap, rb, fb, kTmaTX, kAdjTZ));
+            FWI_TRY(make_map(&A.fvx, f + F_VX * field, nxt, nzt, Bcap, rb, sb, kTmaTX, kAdjTZ));
+            FWI_TRY(make_map(&A.fvz, f + F_VZ * field, nxt, nzt, Bcap, rb, sb, kTmaTX, kAdjTZ));
+            FWI_TRY(make_map(&A.fsxx, f + F_SXX * field, nxt, nzt, Bcap, rb, sb, kTmaTX, kAdjTZ));
+            FWI_TRY(make_map(&A.fszx, f + F_SZX * field, nxt, nzt, Bcap, rb, sb, kTmaTX, kAdjTZ));
+            FWI_TRY(make_map(&A.fszz, f + F_SZZ * field, nxt, nzt, Bcap, rb, sb, kTmaTX, kAdjTZ));
+        }
+        const int ntx = (nxt + kTmaTX - 1) / kTmaTX;
+        const int ntz = (nzt - 2 * fpad + kTmaTZ - 1) / kTmaTZ;
+        tgrid.nb = B;
+        tgrid.ntz = ntz;
+        tgrid.ntiles = B * ntz * ntx;
+        grid_tma = std::max(1, std::min(tgrid.ntiles, num_sms));
+        const int ntz_a = (nzt - 2 * fpad + kAdjTZ - 1) / kAdjTZ;
+        tgrid_a.nb = B;
+        tgrid_a.ntz = ntz_a;
+        tgrid_a.ntiles = B * ntz_a * ntx;
+        grid_tma_a = std::max(1, std::min(tgrid_a.ntiles, num_sms));
+        return FWI_OK;
+    }
+
+    // Forward stress and velocity passes of one state buffer (0 fwd, 1 adj, 2 state n+1).
+    void pass_stress_fwd(int w, const ItemDesc* items, int it, unsigned flags) {
+        if (kmap == 3) tset.stress(dim3(grid_tma), stream, smaps[w], items, tgrid, it, flags, d_err.as<int>());
+        else ks.stress_f(dim3(grid_sf), stream, items, d_tiles_p, ntiles, it, flags, d_err.as<int>());
+    }
+    void pass_velocity(int w, const ItemDesc* items, int it, unsigned flags) {
+        if (kmap == 3) {
+            const unsigned ev = flags & (FL_INJECT | FL_RECORD);
+            tset.velocity(dim3(grid_tma), stream, vmaps[w], items, tgrid, it, flags & ~ev, d_err.as<int>());
+            if (ev) {
+                events_kernel<<<B, 256, 0, stream>>>(items, it, ev);
+                launches_now++;
+            }
+        } else {
+            ks.velocity(dim3(grid_v), stream, items, d_tiles_p, ntiles, it, flags, d_err.as<int>());
+        }
+    }
+
     std::string shape_key() const {
         return "|B" + std::to_string(B) + "|r" + std::to_string(rows.size()) + "|s" +
                std::to_string(slots) + "|st" + std::to_string(strategy) + "|t" + std::to_string(ntiles) +
@@ -793,6 +1021,7 @@ struct Engine {
         d.We = (adj ? d_wr.as<float>() : d_ws.as<float>()) + (size_t)b * field;
         d.ev_col = (adj ? d_evcol_a.as<int>() : d_evcol_f.as<int>()) + (size_t)b * (nxt + 1);
         d.ev = adj ? d_ev_a.as<int2>() : d_ev_f.as<int2>();
+        d.ev_x = adj ? d_evx_a.as<int>() : d_evx_f.as<int>();
         d.inj = adj ? d_resid.as<float>() : d_srcsig.as<float>();
         d.rec = d_rec.as<float>();
         d.store = d_store.p ? d_store.as<float>() + (size_t)b * nft * 5 * nf : nullptr;
@@ -814,12 +1043,19 @@ struct Engine {
     }
 
     // ---- launches ----------------------------------------------------------
+    // Adjoint stress pass with the reference gradient; the TMA kernel reads the
+    // forward fields from the checkpointed working state (fwd_kind 1).
+    void pass_stress_adj(const ItemDesc* items, int it, unsigned flags) {
+        if (kmap == 3 && ckpt_mode())
+            tset.adjoint(dim3(grid_tma_a), stream, amap, items, tgrid_a, it, flags, d_err.as<int>());
+        else
+            ks.stress_a(dim3(grid_sa), stream, items, d_tiles_p, ntiles, it, flags, d_err.as<int>());
+    }
     void step(bool adj, int it, unsigned sflags, unsigned vflags) {
         const ItemDesc* items = adj ? d_items_a.as<ItemDesc>() : d_items_f.as<ItemDesc>();
-        const Tile* tl = d_tiles_p;
-        int* err = d_err.as<int>();
-        (adj ? ks.stress_a : ks.stress_f)(dim3(adj ? grid_sa : grid_sf), stream, items, tl, ntiles, it, sflags, err);
-        ks.velocity(dim3(grid_v), stream, items, tl, ntiles, it, vflags, err);
+        if (adj) pass_stress_adj(items, it, sflags);
+        else pass_stress_fwd(0, items, it, sflags);
+        pass_velocity(adj ? 1 : 0, items, it, vflags);
         launches_now += 2;
     }
 
@@ -856,9 +1092,8 @@ struct Engine {
     int exact_step(int n) {
         CUDA_TRY(cudaMemcpyAsync(d_nxt.p, d_fwd.p, (size_t)B * state * 4, cudaMemcpyDeviceToDevice, stream));
         const ItemDesc* itn = d_items_n.as<ItemDesc>();
-        int* err = d_err.as<int>();
-        ks.stress_f(dim3(grid_sf), stream, itn, d_tiles_p, ntiles, n, 0u, err);
-        ks.velocity(dim3(grid_v), stream, itn, d_tiles_p, ntiles, n, FL_INJECT, err);
+        pass_stress_fwd(2, itn, n, 0u);
+        pass_velocity(2, itn, n, FL_INJECT);
         const long long cells = (long long)(nzt - 2 * fpad) * (nxt - 2 * fpad);
         const dim3 g((unsigned)((cells + kExactThreads - 1) / kExactThreads), (unsigned)B);
         const ItemDesc* ia = d_items_a.as<ItemDesc>();
@@ -1007,8 +1242,6 @@ struct Engine {
         cudaEvent_t a, b;
         CUDA_TRY(cudaEventCreate(&a));
         CUDA_TRY(cudaEventCreate(&b));
-        const Tile* tl = d_tiles_p;
-        int* er = d_err.as<int>();
         const ItemDesc* itf = d_items_f.as<ItemDesc>();
         const ItemDesc* ita = d_items_a.as<ItemDesc>();
         const bool have_adj_src = ckpt_mode() ? true : d_store.p != nullptr;
@@ -1017,10 +1250,13 @@ struct Engine {
             if (adj && !have_adj_src) { ms[k] = 0.0; continue; }
             const int it = fwi_dt * (nft - 1);  // a sampled step: the gradient runs
             auto launch = [&]() {
-                if (k == 0) ks.stress_f(dim3(grid_sf), stream, itf, tl, ntiles, it, 0u, er);
-                if (k == 1) ks.velocity(dim3(grid_v), stream, itf, tl, ntiles, it, FL_INJECT | FL_WE, er);
-                if (k == 2) ks.stress_a(dim3(grid_sa), stream, ita, tl, ntiles, it, FL_GRAD, er);
-                if (k == 3) ks.velocity(dim3(grid_v), stream, ita, tl, ntiles, it, FL_INJECT | FL_WE, er);
+                // the forms of the recompute sweeps (forward) and of the adjoint
+                // sweep; source/receiver events (a separate small kernel in the
+                // TMA mapping) are left out
+                if (k == 0) pass_stress_fwd(0, itf, it, 0u);
+                if (k == 1) pass_velocity(0, itf, it, 0u);
+                if (k == 2) pass_stress_adj(ita, it, FL_GRAD);
+                if (k == 3) pass_velocity(1, ita, it, FL_WE);
             };
             launch();  // warm-up
             CUDA_TRY(cudaEventRecord(a, stream));
@@ -1510,20 +1746,32 @@ int fwi_psv_set_gradient_mode(fwi_psv_engine* h, int mode) {
 
 int fwi_psv_set_exec(fwi_psv_engine* h, int use_graphs, int block_x, int tile_z, int batch) {
     GUARD_ENGINE(h);
-    if ((block_x != 0 && block_x != 32 && block_x != fwi::kTileX) || tile_z < 0 || batch < 0)
-        return fail(FWI_ERR_INVALID, "block_x must be 0, 32 or 128; tile_z and batch >= 0");
+    if ((block_x != 0 && block_x != 32 && block_x != 64 && block_x != fwi::kTileX && block_x != 256) ||
+        tile_z < 0 || batch < 0)
+        return fail(FWI_ERR_INVALID, "block_x must be 0, 32, 64, 128 or 256; tile_z and batch >= 0");
     Engine& e = h->e;
     e.use_graphs = use_graphs ? 1 : 0;
     e.bx_req = block_x;
     e.tz_req = tile_z;
     e.batch_override = batch;
-    // block_x 128 (or a tile height) selects the z-march, block_x 32 the scalar
-    // cell mapping, 0 the default vectorised cells
-    const int map = (block_x == fwi::kTileX || tile_z > 0) ? 0 : (block_x == 32 ? 1 : 2);
+    // block_x 128 (or a tile height) selects the z-march, 32 the scalar cell
+    // mapping, 64 the vectorised cells, 256 the TMA-staged tiles, 0 the default
+    const int map = (block_x == fwi::kTileX || tile_z > 0) ? 0
+                    : block_x == 32                        ? 1
+                    : block_x == 256                       ? 3
+                    : block_x == 64                        ? 2
+                                                           : fwi::kDefaultMap;
     if (map != e.kmap) {
+        if (map == 3) {
+            cudaSetDevice(e.device);
+            cudaError_t ce = e.tset.prepare();
+            if (ce != cudaSuccess)
+                return fail(FWI_ERR_CUDA, std::string("TMA kernels: ") + cudaGetErrorString(ce));
+        }
         e.kmap = map;
         e.ks = fwi::kernels_for(e.fpad, map);
     }
+    e.invalidate_batch();
     for (auto& kv : e.tilesets) kv.second->ntiles = 0;
     e.drop_graphs();
     return FWI_OK;

@@ -70,6 +70,7 @@ struct __align__(16) ItemDesc {
     float *mvx_z, *mvz_z, *mszz_z, *mszx_z;  // [tp][pitch]
     const int* ev_col;                       // [nxt+1] offsets into ev, by column
     const int2* ev;                          // (z, code): code >= 0 inject row, < 0 record row ~code
+    const int* ev_x;                         // column of each ev entry (same indexing as ev)
     const float* inj;                        // [rows][nt]
     float* rec;                              // [rows][nt]
     float* store;                            // [nft][5][nfz][nfx]

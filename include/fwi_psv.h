@@ -222,15 +222,21 @@ int fwi_psv_checkpoint_plan(int nsteps, int slots, int* actions, int cap, int* c
                             long long* forward_steps);
 
 /* Device time of one launch of each hot kernel on the current batch, averaged
- * over `reps` launches timed with CUDA events on the engine's stream:
- * ms[0] forward stress, ms[1] forward velocity (+energy, events), ms[2] adjoint
- * stress (+ux/uz, gradient), ms[3] adjoint velocity.  Needs a prior forward;
- * it overwrites the wavefield state (the retained forward is dropped). */
+ * over `reps` launches timed with CUDA events on the engine's stream, in the
+ * form the checkpointed gradient runs most: ms[0] forward stress, ms[1]
+ * forward velocity (no energy sum: the recompute sweeps), ms[2] adjoint stress
+ * (+ux/uz and the gradient), ms[3] adjoint velocity (+energy).  Source and
+ * receiver events are not included.  Needs a prior forward; it overwrites the
+ * wavefield state (the retained forward is dropped). */
 int fwi_psv_time_kernels(fwi_psv_engine* e, int reps, double ms[4]);
 
 /* Execution options: use_graphs != 0 captures the time loop in CUDA graphs
- * (default 1); block_x (0 or 128, the tile width) and tile_z (rows per tile)
- * set the tile shape; batch = shots per launch of fwi_psv_gradient (0 = automatic). */
+ * (default 1); block_x selects the thread mapping of the stencil passes:
+ * 0 the default (256), 256 TMA-staged 128x16 tiles in persistent CTAs, 64
+ * vectorised cells (float4 per thread), 32 scalar cells, 128 (or tile_z > 0,
+ * rows per tile) the register z-march; batch = shots per launch of
+ * fwi_psv_gradient (0 = automatic).  Every mapping computes the same stencil;
+ * rounding differs between mappings. */
 int fwi_psv_set_exec(fwi_psv_engine* e, int use_graphs, int block_x, int tile_z, int batch);
 
 /* ---- allocation-free misfit ---------------------------------------------- */

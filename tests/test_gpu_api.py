@@ -23,8 +23,9 @@ def _case(nshots=5, order=8):
     return p, obs
 
 
+@pytest.mark.parametrize("bx", [64, 256])
 @pytest.mark.parametrize("batch", [1, 2, 5, 0])
-def test_gradient_subbatches_match_oracle(batch):
+def test_gradient_subbatches_match_oracle(batch, bx):
     p, obs = _case()
     g_ref = [np.zeros((p.nfz, p.nfx)) for _ in range(3)]
     mis_ref = []
@@ -35,7 +36,7 @@ def test_gradient_subbatches_match_oracle(batch):
             g_ref[i] += g[i]
     with Engine(p) as eng:
         eng.set_strategy("binomial", snapshots=6)
-        eng.set_exec(True, 0, 0, batch)
+        eng.set_exec(True, bx, 0, batch)
         g, mis = eng.gradient(list(range(p.nshots)), obs)
         g2, mis2 = eng.gradient(list(range(p.nshots)), None, resident=True)
     np.testing.assert_allclose(mis, mis_ref, rtol=1e-4)

@@ -45,21 +45,22 @@ def _pair(order, fsurf, nshots=1, fwi=(1, 1, 1), nt=150):
     return p, obs
 
 
-def _engine_exact(p, obs, shots, snapshots=8, graphs=True):
+def _engine_exact(p, obs, shots, snapshots=8, graphs=True, bx=0):
     with Engine(p) as eng:
         eng.set_gradient_mode("exact")
         eng.set_strategy("binomial", snapshots=snapshots)
-        eng.set_exec(graphs, 0, 0, 0)
+        eng.set_exec(graphs, bx, 0, 0)
         g, mis = eng.gradient(list(shots), obs)
         st = eng.stats()
     return g, mis, st
 
 
+@pytest.mark.parametrize("bx", [64, 256])
 @pytest.mark.parametrize("order,fsurf", [(2, 0), (4, 0), (4, 1), (8, 0), (8, 1)])
-def test_exact_matches_oracle_exact(order, fsurf):
+def test_exact_matches_oracle_exact(order, fsurf, bx):
     p, obs = _pair(order, fsurf)
     J, gl, gm, gr = O.exact_gradient(p, obs)
-    g, mis, st = _engine_exact(p, obs, [0])
+    g, mis, st = _engine_exact(p, obs, [0], bx=bx)
     assert mis[0] == pytest.approx(J, rel=1e-5)
     for name, gg, go in zip(("lam", "mu", "rho"), g, (gl, gm, gr)):
         assert rel_l2(gg, _window(p, go)) <= 1e-4, name

@@ -18,12 +18,18 @@ SEIS_TOL = 1e-5
 GRAD_TOL = 1e-4
 
 
+# block_x of set_exec: 64 = vectorised cells, 256 = TMA-staged tiles (the default)
+MAPPINGS = [64, 256]
+
+
+@pytest.mark.parametrize("bx", MAPPINGS)
 @pytest.mark.parametrize("name", ["ref_o2.npz", "ref_o2_fsurf.npz", "ref_o2_multi.npz"])
-def test_engine_matches_reference_golden(name):
+def test_engine_matches_reference_golden(name, bx):
     p, d = load(name)
     shot = int(d["shot"])
     rows = O.shot_rows(p, shot)
     with Engine(p) as eng:
+        eng.set_exec(True, bx, 0)
         rec, mis = eng.forward([shot], d["obs"], keep=True)
         assert rel_l2(rec[rows], d["out_rec"][rows]) <= SEIS_TOL
         assert mis[0] == pytest.approx(float(d["out_misfit"]), rel=1e-4)
@@ -98,17 +104,41 @@ def _oracle_case(order, fsurf=0, fwi=(1, 1, 1), nt=200, seed=0):
 
 
 @pytest.mark.parametrize("order,fsurf,fwi", [(4, 0, (1, 1, 1)), (6, 0, (2, 1, 1)), (8, 0, (1, 1, 1)),
-                                             (8, 1, (3, 2, 2)), (12, 0, (1, 1, 1)), (4, 1, (1, 1, 1))])
-def test_engine_matches_oracle_higher_orders(order, fsurf, fwi):
+                                             (8, 1, (3, 2, 2)), (12, 0, (1, 1, 1)), (4, 1, (1, 1, 1)),
+                                             (2, 1, (1, 1, 1)), (10, 1, (1, 2, 1))])
+@pytest.mark.parametrize("bx", MAPPINGS)
+def test_engine_matches_oracle_higher_orders(order, fsurf, fwi, bx):
     p, obs = _oracle_case(order, fsurf, fwi)
     J, g_o, fw_o, ad_o = O.gradient(p, obs, 0)
     with Engine(p) as eng:
+        eng.set_exec(True, bx, 0)
         rec, mis = eng.forward([0], obs, keep=True)
         assert rel_l2(rec[: p.nrec], fw_o["rec"]) <= SEIS_TOL
         assert mis[0] == pytest.approx(J, rel=1e-4)
         g = eng.backward()
     for i in range(3):
         assert rel_l2(g[i][0], g_o[i]) <= GRAD_TOL, i
+
+
+@pytest.mark.parametrize("bx", MAPPINGS)
+@pytest.mark.parametrize("order,fsurf,fwi", [(2, 0, (1, 1, 1)), (4, 1, (1, 1, 1)), (8, 0, (2, 1, 1)),
+                                             (8, 1, (3, 2, 2)), (12, 0, (1, 1, 1))])
+def test_checkpointed_adjoint_matches_oracle(order, fsurf, fwi, bx):
+    """Binomial checkpointing: the adjoint stress pass reads the forward fields
+    from the recomputed forward state (the TMA mapping stages them)."""
+    p, obs = _oracle_case(order, fsurf, fwi, nt=160, seed=8)
+    J, g_o, fw_o, ad_o = O.gradient(p, obs, 0)
+    with Engine(p) as eng:
+        eng.set_exec(True, bx, 0)
+        eng.set_strategy("binomial", snapshots=5)
+        rec, mis = eng.forward([0], obs, keep=True)
+        g = eng.backward()
+        ws, wr = eng.energy(0)
+    assert rel_l2(rec[: p.nrec], fw_o["rec"]) <= SEIS_TOL
+    assert mis[0] == pytest.approx(J, rel=1e-4)
+    for i in range(3):
+        assert rel_l2(g[i][0], g_o[i]) <= GRAD_TOL, i
+    assert rel_l2(wr, ad_o["We"]) <= GRAD_TOL
 
 
 def test_batch_equals_single_shots_bitwise():
@@ -131,10 +161,16 @@ def test_batch_equals_single_shots_bitwise():
             np.testing.assert_allclose(g_sum[i], g_b[i].sum(0), rtol=1e-5, atol=1e-30)
 
 
+@pytest.mark.parametrize("bx", MAPPINGS)
 @pytest.mark.parametrize("fwi,snaps", [((1, 1, 1), 3), ((3, 2, 2), 2), ((1, 1, 1), 0), ((2, 1, 1), 40)])
-def test_binomial_checkpointing_equals_full_storage(fwi, snaps):
+def test_binomial_checkpointing_equals_full_storage(fwi, snaps, bx):
+    """Same forward; the gradient is bitwise equal where both strategies run
+    the same adjoint kernel (vectorised mapping).  The TMA mapping stages the
+    checkpointed forward state in its own adjoint kernel, whose rounding
+    differs from the full-storage kernel's."""
     p, obs = _oracle_case(8, 0, fwi, nt=150, seed=3)
     with Engine(p) as eng:
+        eng.set_exec(True, bx, 0)
         eng.set_strategy("full")
         rec_f, mis_f = eng.forward([0], obs, keep=True)
         g_f = eng.backward()
@@ -144,7 +180,10 @@ def test_binomial_checkpointing_equals_full_storage(fwi, snaps):
         st = eng.stats()
     assert np.array_equal(rec_f, rec_c) and mis_f[0] == mis_c[0]
     for i in range(3):
-        assert np.array_equal(g_f[i], g_c[i]), i
+        if bx == 64:
+            assert np.array_equal(g_f[i], g_c[i]), i
+        else:
+            assert rel_l2(g_c[i], g_f[i]) <= 3e-5, i
     assert st["recompute_steps"] > 0
 
 
@@ -162,10 +201,10 @@ def test_graphs_and_direct_launches_agree():
         assert np.array_equal(out[0][1][i], out[1][1][i])
 
 
-@pytest.mark.parametrize("bx,tz", [(128, 1), (128, 5), (128, 64), (32, 0)])
+@pytest.mark.parametrize("bx,tz", [(128, 1), (128, 5), (128, 64), (32, 0), (64, 0), (256, 0)])
 def test_thread_mappings_agree(bx, tz):
-    """z-march tiles of any height, the scalar cell mapping and the default
-    vectorised mapping compute the same stencil (rounding may differ)."""
+    """z-march tiles of any height, the scalar and vectorised cell mappings and
+    the TMA-staged tiles compute the same stencil (rounding may differ)."""
     p, obs = _oracle_case(8, 0, (1, 1, 1), nt=100, seed=6)
     with Engine(p) as eng:
         rec0, _ = eng.forward([0], obs, keep=True)
@@ -174,8 +213,10 @@ def test_thread_mappings_agree(bx, tz):
         rec1, _ = eng.forward([0], obs, keep=True)
         g1 = eng.backward()
     assert rel_l2(rec1, rec0) <= 1e-6
+    # two FP32 roundings of the same 100-step correlation sums (each mapping
+    # is within 1e-4 of the FP64 oracle on its own)
     for i in range(3):
-        assert rel_l2(g1[i], g0[i]) <= 1e-5
+        assert rel_l2(g1[i], g0[i]) <= 3e-5
 
 
 def test_z_march_tile_heights_bitwise_identical():
@@ -203,7 +244,7 @@ def test_error_paths():
             eng.set_sources(bad_x, p.src_z, p.src_comp, p.src_shot, p.src_signal)
         assert e.value.code == "FWI_ERR_INVALID"
         with pytest.raises(_capi.FwiError) as e:
-            eng.set_exec(True, 64, 0)
+            eng.set_exec(True, 48, 0)
         assert e.value.code == "FWI_ERR_INVALID"
         with pytest.raises(_capi.FwiError) as e:
             eng.forward([0], obs * 1e12 + 1e11)
