@@ -54,6 +54,25 @@ class Stats(C.Structure):
         ("h2d_bytes", C.c_int64), ("d2h_bytes", C.c_int64), ("batch", C.c_int64)]
 
 
+class Layout(C.Structure):
+    _fields_ = [(n, C.c_int) for n in ("nt", "nzt", "nxt", "fpad", "ppad", "npml", "fsurf", "fdorder",
+                                        "fwi_dt", "fwi_dx", "fwi_dz", "x1", "x2", "z1", "z2", "nfz", "nfx",
+                                        "device")]
+
+
+class FwiOpts(C.Structure):
+    _fields_ = [("max_iter", C.c_int), ("max_error", C.c_double), ("step_length", C.c_double),
+                ("order", C.c_int), ("trial_misfit", C.c_int), ("precondition", C.c_int),
+                ("true_lam", dp), ("true_mu", dp), ("true_rho", dp)]
+
+
+class FwiIter(C.Structure):
+    _fields_ = [("misfit", C.c_double), ("step_length", C.c_double), ("trials", C.c_int), ("status", C.c_int),
+                ("model_error", C.c_double), ("seconds", C.c_double)]
+
+
+TRIAL_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_double, dp)
+
 _lib = None
 
 # (name, restype, argtypes); every int-returning function is a status call.
@@ -87,6 +106,14 @@ _SIGS = {
     "fwi_psv_time_kernels": (C.c_int, [C.c_void_p, C.c_int, dp]),
     "fwi_psv_misfit_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_double,
                                          C.c_void_p, dp, C.c_void_p]),
+    "fwi_psv_get_layout": (C.c_int, [C.c_void_p, C.POINTER(Layout)]),
+    "fwi_psv_set_model_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "fwi_psv_set_precondition": (C.c_int, [C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_double]),
+    "fwi_psv_misfit": (C.c_int, [C.c_void_p, C.c_int, ip, dp, dp, C.c_int]),
+    "fwi_psv_fwi_run": (C.c_int, [C.c_void_p, C.POINTER(FwiOpts), C.c_int, ip, dp, dp, dp, dp,
+                                  C.POINTER(FwiIter), ip]),
+    "fwi_psv_calc_opt_step": (C.c_double, [dp, dp]),
+    "fwi_psv_step_search": (C.c_int, [C.c_double, C.c_double, TRIAL_FN, C.c_void_p, dp, ip, ip]),
     "fwi_psv_forward_kernel": (C.c_int, [C.c_int] * 6 + [C.c_double] * 3 + [C.c_int, C.c_int, dp, C.c_int]
                                + [dp] * 6 + [dp] * 5 + [C.c_int] + [dp] * 6 + [dp] * 8
                                + [C.c_int, ip, ip, ip, dp, ip] + [C.c_int, ip, ip, ip, dp, ip]

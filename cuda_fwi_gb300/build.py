@@ -22,7 +22,7 @@ LIB = OUT_DIR / "libfwi_psv.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O2,-ffp-contract=off",
            "--expt-relaxed-constexpr", f"-I{ROOT / 'include'}", f"-I{CSRC}"]
-UNITS = ["fwi_engine.cu", "fwi_host.cpp", "fwi_refshim.cpp", "fwi_noalloc.cu"]
+UNITS = ["fwi_engine.cu", "fwi_host.cpp", "fwi_refshim.cpp", "fwi_noalloc.cu", "fwi_optim.cu"]
 HEADERS = ["fwi_kernels.cuh", "fwi_host.h"]
 
 

@@ -110,6 +110,81 @@ __global__ void events_kernel(const ItemDesc* __restrict__ items, int it, unsign
         }
 }
 
+// FDMedium::average_parameters (fd_medium.cu:128-159) on the device, fused
+// with the dt scaling of the engine's material layout: FP64 lam, mu, rho
+// [nzt][nxt] -> FP32 L, M2, MZX, BX, BZ [nzt][pitch].  Same FP64 expressions
+// as the host path (fwi_host.cpp), so both give identical materials.
+__global__ void materials_kernel(const double* __restrict__ lam, const double* __restrict__ mu,
+                                 const double* __restrict__ rho, int nzt, int nxt, int pitch, int fpad,
+                                 double dt, float* __restrict__ mat, size_t field, int* __restrict__ zero_mu) {
+    const size_t n = (size_t)nzt * nxt;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const int iz = (int)(i / nxt), ix = (int)(i % nxt);
+        const size_t o = (size_t)iz * pitch + ix;
+        mat[o] = (float)(dt * lam[i]);
+        mat[field + o] = (float)(2.0 * dt * mu[i]);
+        if (mu[i] == 0.0 && iz >= fpad && iz < nzt - fpad && ix >= fpad && ix < nxt - fpad) atomicOr(zero_mu, 1);
+        float mz = 0.f, bx = 0.f, bz = 0.f;
+        if (iz < nzt - 1 && ix < nxt - 1) {
+            const double m00 = mu[i], m01 = mu[i + 1], m10 = mu[i + nxt], m11 = mu[i + nxt + 1];
+            const bool zero = m00 == 0.0 || m01 == 0.0 || m10 == 0.0 || m11 == 0.0;
+            const double h = zero ? 0.0 : 4.0 / ((1.0 / m00) + (1.0 / m01) + (1.0 / m10) + (1.0 / m11));
+            const double r00 = rho[i], r10 = rho[i + nxt], r01 = rho[i + 1];
+            double rzp = 1.0 / (0.5 * (r00 + r10));
+            const double rxp = 1.0 / (0.5 * (r00 + r01));
+            if (r00 < 1e-4 && r10 < 1e-4) rzp = 0.0;
+            if (r00 < 1e-4 && r01 < 1e-4) rzp = 0.0;  // the reference's second guard (fd_medium.cu:152-154)
+            mz = (float)(dt * h);
+            bx = (float)(dt * rxp);
+            bz = (float)(dt * rzp);
+        }
+        mat[2 * field + o] = mz;
+        mat[3 * field + o] = bx;
+        mat[4 * field + o] = bz;
+    }
+}
+
+// Energy weights of one batch slot per blockIdx.y (fd_wave_model.cu:1004-1052):
+// the largest sqrt(Ws * Wr) over the FWI window samples (non-negative, so the
+// float bits order like the values).
+__global__ void we_max_kernel(const ItemDesc* __restrict__ items, const float* __restrict__ ws,
+                              const float* __restrict__ wr, size_t field, unsigned* __restrict__ wmax) {
+    const int b = blockIdx.y;
+    const ItemDesc& D = items[b];
+    const size_t nf = (size_t)D.nfz * D.nfx;
+    float m = 0.f;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < nf; i += (size_t)gridDim.x * blockDim.x) {
+        const int zf = (int)(i / D.nfx), xf = (int)(i % D.nfx);
+        const int iz = D.wz1 + zf * D.fwi_dz, ix = D.wx1 + xf * D.fwi_dx;
+        if (iz >= D.wz2 || ix >= D.wx2) continue;
+        const size_t c = (size_t)b * field + (size_t)iz * D.pitch + ix;
+        m = fmaxf(m, (float)sqrt((double)ws[c] * (double)wr[c]));
+    }
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(wmax + b, __float_as_uint(m));
+}
+
+// Divide each slot's gradient by its regularised energy weight
+// sqrt(Ws Wr) + 0.005 max; the constant 1/C^2 factors are applied in FP64
+// when the gradients leave the device (FP32 would underflow them).
+__global__ void precondition_kernel(const ItemDesc* __restrict__ items, const float* __restrict__ ws,
+                                    const float* __restrict__ wr, size_t field, const unsigned* __restrict__ wmax) {
+    const int b = blockIdx.y;
+    const ItemDesc& D = items[b];
+    const size_t nf = (size_t)D.nfz * D.nfx;
+    const double reg = 0.005 * (double)__uint_as_float(wmax[b]);
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < nf; i += (size_t)gridDim.x * blockDim.x) {
+        const int zf = (int)(i / D.nfx), xf = (int)(i % D.nfx);
+        const int iz = D.wz1 + zf * D.fwi_dz, ix = D.wx1 + xf * D.fwi_dx;
+        if (iz >= D.wz2 || ix >= D.wx2) continue;
+        const size_t c = (size_t)b * field + (size_t)iz * D.pitch + ix;
+        const double we = sqrt((double)ws[c] * (double)wr[c]) + reg;
+        D.glam[i] = (float)((double)D.glam[i] / we);
+        D.gmu[i] = (float)((double)D.gmu[i] / we);
+        D.grho[i] = (float)((double)D.grho[i] / we);
+    }
+}
+
 // sum the per-shot gradient triples: out[i] = sum_b in[b*n + i]
 __global__ void sum_shots_kernel(const float* __restrict__ in, float* __restrict__ out, size_t n,
                                  int nb, int accumulate) {
@@ -431,6 +506,11 @@ struct Engine {
     TmaGrid tgrid{}, tgrid_a{};
     int grid_tma = 1, grid_tma_a = 1;
     bool zero_mu = false;  // some interior cell has mu == 0 (exact mode unsupported)
+    // energy-weight preconditioning of each shot's gradient (fd_wave_model.cu:1004-1052)
+    bool pre_on = false;
+    double pre_c[3] = {1.0, 1.0, 1.0};  // C_lam, C_mu, C_rho
+    DBuf d_wmax;
+    double out_scale(int q) const { return pre_on ? 1.0 / (pre_c[q] * pre_c[q]) : 1.0; }
     HBuf h_stage, h_rec, h_grad;
     DBuf d_err;  // kernel error flags (bounded waits that timed out)
     bool obs_valid = false;
@@ -570,6 +650,27 @@ struct Engine {
         CUDA_TRY(cudaMemcpyAsync(d_mat.p, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice,
                                  stream));
         CUDA_TRY(cudaStreamSynchronize(stream));
+        have_model = true;
+        return FWI_OK;
+    }
+
+    // Raw FP64 models already on the device; averages and dt scaling by a kernel.
+    int set_model_device(const double* dl, const double* dm, const double* dr) {
+        if (!dl || !dm || !dr) return fail(FWI_ERR_INVALID, "null material array");
+        FWI_TRY(bind());
+        FWI_TRY(d_mat.ensure(5 * field * sizeof(float)));
+        FWI_TRY(d_blow.ensure(16));
+        CUDA_TRY(cudaMemsetAsync(d_mat.p, 0, 5 * field * sizeof(float), stream));
+        CUDA_TRY(cudaMemsetAsync(d_blow.p, 0, 4, stream));
+        const size_t n = (size_t)nzt * nxt;
+        const int blocks = (int)std::min<size_t>((n + 255) / 256, (size_t)num_sms * 8);
+        materials_kernel<<<blocks, 256, 0, stream>>>(dl, dm, dr, nzt, nxt, pitch, fpad, dt, d_mat.as<float>(),
+                                                     field, d_blow.as<int>());
+        CUDA_TRY(cudaGetLastError());
+        int z = 0;
+        CUDA_TRY(cudaMemcpyAsync(&z, d_blow.p, 4, cudaMemcpyDeviceToHost, stream));
+        CUDA_TRY(cudaStreamSynchronize(stream));
+        zero_mu = z != 0;
         have_model = true;
         return FWI_OK;
     }
@@ -1348,6 +1449,16 @@ struct Engine {
             }
             return FWI_OK;
         }));
+        if (pre_on) {
+            FWI_TRY(d_wmax.ensure((size_t)std::max(B, 1) * sizeof(unsigned)));
+            CUDA_TRY(cudaMemsetAsync(d_wmax.p, 0, (size_t)B * sizeof(unsigned), stream));
+            const dim3 g((unsigned)std::min<size_t>((nf + 255) / 256, 1024), (unsigned)B);
+            we_max_kernel<<<g, 256, 0, stream>>>(d_items_a.as<ItemDesc>(), d_ws.as<float>(), d_wr.as<float>(), field,
+                                                d_wmax.as<unsigned>());
+            precondition_kernel<<<g, 256, 0, stream>>>(d_items_a.as<ItemDesc>(), d_ws.as<float>(), d_wr.as<float>(),
+                                                       field, d_wmax.as<unsigned>());
+            launches_now += 2;
+        }
         if (accumulate) {
             sum_shots_kernel<<<592, 256, 0, stream>>>(d_grad.as<float>(), d_gacc.as<float>(), 3 * nf, B, 1);
             launches_now++;
@@ -1376,12 +1487,13 @@ struct Engine {
         stats.launches = launches_now;
         stats.adjoint_steps = nt;
         stats.recompute_steps = ckpt_mode() ? (recompute > 0 ? recompute : plan_cost) * unit() : 0;
+        const double k0 = out_scale(0), k1 = out_scale(1), k2 = out_scale(2);
         for (size_t s = 0; s < ntrip && want; s++)
             for (size_t i = 0; i < nf; i++) {
                 const float* t = g + s * 3 * nf;
-                if (gl) gl[s * nf + i] = t[i];
-                if (gm) gm[s * nf + i] = t[nf + i];
-                if (gr) gr[s * nf + i] = t[2 * nf + i];
+                if (gl) gl[s * nf + i] = t[i] * k0;
+                if (gm) gm[s * nf + i] = t[nf + i] * k1;
+                if (gr) gr[s * nf + i] = t[2 * nf + i] * k2;
             }
         bwd_done = true;
         return FWI_OK;
@@ -1439,10 +1551,11 @@ struct Engine {
             CUDA_TRY(cudaMemcpyAsync(h_grad.p, d_gacc.p, 3 * nf * 4, cudaMemcpyDeviceToHost, stream));
         CUDA_TRY(cudaStreamSynchronize(stream));
         const float* g = h_grad.as<float>();
+        const double k0 = out_scale(0), k1 = out_scale(1), k2 = out_scale(2);
         for (size_t i = 0; want && i < nf; i++) {
-            if (gl) gl[i] = g[i];
-            if (gm) gm[i] = g[nf + i];
-            if (gr) gr[i] = g[2 * nf + i];
+            if (gl) gl[i] = g[i] * k0;
+            if (gm) gm[i] = g[nf + i] * k1;
+            if (gr) gr[i] = g[2 * nf + i] * k2;
         }
         stats.last_forward_ms = fwd_ms;
         stats.last_backward_ms = bwd_ms;
@@ -1455,6 +1568,38 @@ struct Engine {
         stats.h2d_bytes = h2d;
         stats.d2h_bytes = (misfit ? 0 : 0) + (want ? (int64_t)(3 * nf * 4) : 0) +
                           (int64_t)(rows_cap * 8) * ((n + bs - 1) / bs);
+        stats.batch = bs;
+        return FWI_OK;
+    }
+
+    // Misfits of n shots by forward-only runs in sub-batches (no storage, no
+    // checkpoints): the trial runs of the step-length search.
+    int misfit_only(int n, const int* ids, const double* obs, double* misfit, int flags) {
+        FWI_TRY(bind());
+        if (n < 1 || !ids || !misfit) return fail(FWI_ERR_INVALID, "empty shot list or null misfit");
+        const bool resident = (flags & FWI_FWD_RESIDENT_OBS) != 0;
+        if (!resident && !obs) return fail(FWI_ERR_INVALID, "observed data required");
+        if (resident && !obs_valid) return fail(FWI_ERR_STATE, "no observed data resident on the device");
+        if (!resident) {
+            std::vector<int> recs;
+            for (int r = 0; r < nrec; r++) {
+                if (rcomp[r] != 2) continue;
+                for (int b = 0; b < n; b++)
+                    if (rshot[r] == ids[b]) { recs.push_back(r); break; }
+            }
+            FWI_TRY(upload_obs(obs, recs));
+        }
+        const int bs = batch_override > 0 ? std::min(batch_override, n) : auto_batch(n);
+        double ms = 0;
+        int64_t launches = 0;
+        for (int k = 0; k < n; k += bs) {
+            const int m = std::min(bs, n - k);
+            FWI_TRY(forward(m, ids + k, nullptr, nullptr, misfit + k, FWI_FWD_RESIDENT_OBS));
+            ms += stats.last_forward_ms;
+            launches += stats.launches;
+        }
+        stats.last_forward_ms = ms;
+        stats.launches = launches;
         stats.batch = bs;
         return FWI_OK;
     }
@@ -1702,6 +1847,38 @@ int fwi_psv_set_model_lmr(fwi_psv_engine* h, const double* lam, const double* mu
     std::vector<double> mz(na), rz(na), rx(na);
     fwi::average_parameters(e.nzt, e.nxt, mu, rho, mz.data(), rz.data(), rx.data());
     return e.set_model(lam, mu, mz.data(), rz.data(), rx.data());
+}
+
+int fwi_psv_get_layout(fwi_psv_engine* h, fwi_psv_layout* o) {
+    GUARD_ENGINE(h);
+    if (!o) return fail(FWI_ERR_INVALID, "null layout");
+    const Engine& e = h->e;
+    *o = {e.nt, e.nzt, e.nxt, e.fpad, e.ppad, e.npml, e.fsurf, e.fdorder, e.fwi_dt, e.fwi_dx, e.fwi_dz,
+          e.wx1, e.wx2, e.wz1, e.wz2, e.nfz, e.nfx, e.device};
+    return FWI_OK;
+}
+
+int fwi_psv_set_model_device(fwi_psv_engine* h, const double* d_lam, const double* d_mu, const double* d_rho) {
+    GUARD_ENGINE(h);
+    return h->e.set_model_device(d_lam, d_mu, d_rho);
+}
+
+int fwi_psv_set_precondition(fwi_psv_engine* h, int on, double c_lam, double c_mu, double c_rho) {
+    GUARD_ENGINE(h);
+    if (on && (!(c_lam > 0) || !(c_mu > 0) || !(c_rho > 0)))
+        return fail(FWI_ERR_INVALID, "preconditioning needs positive medium averages");
+    Engine& e = h->e;
+    e.pre_on = on != 0;
+    e.pre_c[0] = c_lam;
+    e.pre_c[1] = c_mu;
+    e.pre_c[2] = c_rho;
+    return FWI_OK;
+}
+
+int fwi_psv_misfit(fwi_psv_engine* h, int nshots, const int* shots, const double* obs, double* misfit,
+                   int flags) {
+    GUARD_ENGINE(h);
+    return h->e.misfit_only(nshots, shots, obs, misfit, flags);
 }
 
 int fwi_psv_set_sources(fwi_psv_engine* h, int n, const int* x, const int* z, const int* comp,

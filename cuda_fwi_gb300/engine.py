@@ -141,6 +141,45 @@ class Engine:
                                            *[pd(x) for x in g], flags), "gradient")
         return (tuple(g) if want else None), mis
 
+    def misfit(self, shots, obs=None, resident=False):
+        """Per-shot misfits from forward-only runs (the step-length trials)."""
+        ids = _i32(shots)
+        mis = np.zeros(len(ids))
+        o = None if resident else _f64(obs)
+        check(_capi.lib().fwi_psv_misfit(self.h, len(ids), pi(ids), pd(o), pd(mis),
+                                         _capi.FWI_FWD_RESIDENT_OBS if resident else 0), "misfit")
+        return mis
+
+    def set_precondition(self, on=True, c=(1.0, 1.0, 1.0)):
+        """Energy-weight preconditioning of each shot's gradient with medium
+        averages c = (C_lam, C_mu, C_rho)."""
+        check(_capi.lib().fwi_psv_set_precondition(self.h, int(on), *[float(x) for x in c]), "set_precondition")
+
+    def set_model_device(self, lam, mu, rho):
+        """lam, mu, rho: CUDA float64 tensors [nzt][nxt] on the engine's device."""
+        for t in (lam, mu, rho):
+            assert t.is_cuda and t.dtype == __import__("torch").float64 and t.is_contiguous()
+        check(_capi.lib().fwi_psv_set_model_device(self.h, C.c_void_p(lam.data_ptr()), C.c_void_p(mu.data_ptr()),
+                                                   C.c_void_p(rho.data_ptr())), "set_model_device")
+
+    def fwi_run(self, shots, obs, max_iter, step_length=0.01, max_error=0.0, order="summed", trial="sum",
+                precondition=True, model=None, true_model=None):
+        """The inversion loop on the device.  model = (lam, mu, rho) start
+        (default: the problem's); returns ((lam, mu, rho), log) with one dict
+        per update (misfit, step_length, trials, status, model_error, seconds)."""
+        ids = _i32(shots)
+        lam, mu, rho = [np.array(x, np.float64, order="C") for x in (model or (self.p.lam, self.p.mu, self.p.rho))]
+        tm = [_f64(x) for x in true_model] if true_model is not None else [None] * 3
+        o = _capi.FwiOpts(max_iter, max_error, step_length, {"summed": 0, "per_shot": 1}[order],
+                          {"sum": 0, "last": 1}[trial], int(precondition), pd(tm[0]), pd(tm[1]), pd(tm[2]))
+        n = max_iter * (len(ids) if order == "per_shot" else 1)
+        log = (_capi.FwiIter * max(n, 1))()
+        done = C.c_int()
+        check(_capi.lib().fwi_psv_fwi_run(self.h, C.byref(o), len(ids), pi(ids), pd(_f64(obs)), pd(lam), pd(mu),
+                                          pd(rho), log, C.byref(done)), "fwi_run")
+        out = [{k: getattr(log[i], k) for k, _ in _capi.FwiIter._fields_} for i in range(done.value)]
+        return (lam, mu, rho), out
+
     def time_kernels(self, reps=20):
         """Average device ms of one launch of: forward stress, forward velocity,
         adjoint stress, adjoint velocity (drops the retained forward)."""

@@ -239,6 +239,91 @@ int fwi_psv_time_kernels(fwi_psv_engine* e, int reps, double ms[4]);
  * rounding differs between mappings. */
 int fwi_psv_set_exec(fwi_psv_engine* e, int use_graphs, int block_x, int tile_z, int batch);
 
+/* Grid and FWI-window extents of an engine (after fwi_psv_set_fwi). */
+typedef struct fwi_psv_layout {
+    int nt, nzt, nxt, fpad, ppad, npml, fsurf, fdorder;
+    int fwi_dt, fwi_dx, fwi_dz, x1, x2, z1, z2, nfz, nfx;
+    int device;
+} fwi_psv_layout;
+int fwi_psv_get_layout(fwi_psv_engine* e, fwi_psv_layout* out);
+
+/* ---- device-resident models, preconditioning, trial misfits --------------- */
+
+/* lam, mu, rho [nzt][nxt] FP64 already in device memory (cudaMalloc'd by the
+ * caller, current device = the engine's); the staggered averages
+ * (FDMedium::average_parameters, fd_medium.cu:128-159) and the dt scaling run
+ * as a kernel, giving the same materials as fwi_psv_set_model_lmr. */
+int fwi_psv_set_model_device(fwi_psv_engine* e, const double* d_lam, const double* d_mu,
+                             const double* d_rho);
+
+/* Energy-weight preconditioning of each shot's gradient before the shot sum
+ * (scale_gradients_with_energy_weights, fd_wave_model.cu:1004-1052):
+ * g /= (sqrt(Ws Wr) + 0.005 max sqrt(Ws Wr)) C^2 with Ws, Wr the forward and
+ * adjoint energy sums of that shot and C the medium averages
+ * (FDMedium::medium_average, fd_medium.cu:253-277). on = 0 switches it off. */
+int fwi_psv_set_precondition(fwi_psv_engine* e, int on, double c_lam, double c_mu, double c_rho);
+
+/* Per-shot misfits of `nshots` shots from forward-only runs in sub-batches
+ * (no storage, no checkpoints): the trial runs of the step-length search.
+ * obs and flags as for fwi_psv_gradient. */
+int fwi_psv_misfit(fwi_psv_engine* e, int nshots, const int* shots, const double* obs, double* misfit,
+                   int flags);
+
+/* ---- FWI optimiser ---------------------------------------------------------
+ * The reference's inversion loop (FDWaveModel::fwi_simulate, fd_wave_model.cu
+ * :736-955) on the device: medium averages, batched checkpointed gradients
+ * with energy-weight preconditioning, the parabolic step-length search
+ * (fwi_step_length_estimation.cu:16-223) with batched forward-only trials,
+ * and the bounded, max-normalised material update (FDMedium::fwi_grad_update,
+ * fd_medium.cu:161-240: rho in [1.5, 3000] with half the step, lam <= 48e9,
+ * mu <= 27e9).  Gradients, models and updates stay on the device; the host
+ * runs the search's control flow.  Differences from the reference, each
+ * selectable: FWI_ORDER_SUMMED sums the shot gradients before one update per
+ * iteration (the reference updates after every shot: FWI_ORDER_PER_SHOT);
+ * FWI_TRIAL_SUM compares misfits summed over all shots in the search (the
+ * reference keeps only the last shot's: FWI_TRIAL_LAST_SHOT).  The update
+ * touches the FWI window's sample cells; a failed search stops the loop with
+ * the model unchanged instead of exiting the process. */
+enum { FWI_ORDER_SUMMED = 0, FWI_ORDER_PER_SHOT = 1 };
+enum { FWI_TRIAL_SUM = 0, FWI_TRIAL_LAST_SHOT = 1 };
+typedef struct fwi_psv_fwi_opts {
+    int max_iter;          /* [FDM] max_iteration */
+    double max_error;      /* [FDM] max_error: stop once the misfit falls below it */
+    double step_length;    /* first step-length estimate (the reference starts at 0.01) */
+    int order;             /* FWI_ORDER_* */
+    int trial_misfit;      /* FWI_TRIAL_* */
+    int precondition;      /* energy-weight preconditioning (the reference: 1) */
+    const double *true_lam, *true_mu, *true_rho; /* optional [nzt][nxt]: model error per iteration */
+} fwi_psv_fwi_opts;
+typedef struct fwi_psv_fwi_iter {
+    double misfit;         /* summed shot misfit at the model the gradient was taken at */
+    double step_length;    /* step of the parabolic fit (0 when the search failed) */
+    int trials;            /* trial forward sweeps (over all shots) of the search */
+    int status;            /* 0; 1 no step reduced the misfit (model kept); 2 no bracketing third step */
+    double model_error;    /* ||m - m_true|| / ||m_true|| over lam, mu, rho (each relative), or -1 */
+    double seconds;        /* wall time of the iteration */
+} fwi_psv_fwi_iter;
+/* lam, mu, rho [nzt][nxt]: starting model in, final model out.  log holds
+ * max_iter entries (max_iter * shots for FWI_ORDER_PER_SHOT); *done = entries
+ * written.  obs [nrec][nt] as for fwi_psv_gradient. */
+int fwi_psv_fwi_run(fwi_psv_engine* e, const fwi_psv_fwi_opts* opts, int nshots, const int* shots,
+                    const double* obs, double* lam, double* mu, double* rho, fwi_psv_fwi_iter* log,
+                    int* done);
+
+/* Parabola through (sl[i], L2[i]), i = 0..2, and its vertex -x1/(2 x2)
+ * (calc_opt_step + solvelin, fwi_step_length_estimation.cu:226-271 and
+ * solvelin.cu:6-42, float multiplier and back-substitution accumulator kept). */
+double fwi_psv_calc_opt_step(const double L2[3], const double sl[3]);
+
+/* The step-length search's state machine (fwi_step_length_estimation.cu:46-223)
+ * with a caller-supplied trial: trial(ctx, step, &misfit) evaluates the model
+ * updated with `step` (rho with half of it).  L2_0 = misfit at step 0.  On
+ * return *opt = optimum step (status 0 or 2) and *trials = trial calls;
+ * status 1: no step reduced the misfit within 6 halvings (*opt = 0). */
+typedef int (*fwi_psv_trial_fn)(void* ctx, double step, double* misfit);
+int fwi_psv_step_search(double est, double L2_0, fwi_psv_trial_fn trial, void* ctx, double* opt,
+                        int* trials, int* status);
+
 /* ---- allocation-free misfit ---------------------------------------------- */
 
 /* No counterpart in the reference (whose misfit, calculate_l2_adjoint_sources,
