@@ -106,6 +106,8 @@ _SIGS = {
     "fwi_psv_time_kernels": (C.c_int, [C.c_void_p, C.c_int, dp]),
     "fwi_psv_misfit_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_double,
                                          C.c_void_p, dp, C.c_void_p]),
+    "fwi_psv_set_snapshots": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
+    "fwi_psv_snapshot": (C.c_int, [C.c_void_p, C.c_int, C.c_int, dp]),
     "fwi_psv_get_layout": (C.c_int, [C.c_void_p, C.POINTER(Layout)]),
     "fwi_psv_set_model_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "fwi_psv_set_precondition": (C.c_int, [C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_double]),

@@ -1,7 +1,9 @@
 """Build ``libfwi_psv.so`` (the sm_103a engine + C ABI) in-tree with nvcc.
 
-Output: ``cuda_fwi_gb300/_lib/libfwi_psv.so``.  Translation units are compiled
-in parallel and only when a source is newer than its object.
+Output: ``cuda_fwi_gb300/_lib/libfwi_psv.so`` and the INI-driven host program
+``cuda_fwi_gb300/_lib/fwi_run`` (app/, plain C++ against the C ABI).
+Translation units are compiled in parallel and only when a source is newer
+than its object.
 """
 from __future__ import annotations
 
@@ -23,7 +25,9 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O2,-ffp-contract=off",
            "--expt-relaxed-constexpr", f"-I{ROOT / 'include'}", f"-I{CSRC}"]
 UNITS = ["fwi_engine.cu", "fwi_host.cpp", "fwi_refshim.cpp", "fwi_noalloc.cu", "fwi_optim.cu"]
-HEADERS = ["fwi_kernels.cuh", "fwi_host.h"]
+HEADERS = ["fwi_kernels.cuh", "fwi_exact.cuh", "fwi_tma.cuh", "fwi_host.h"]
+APP_DIR = PKG / "app"
+APP = OUT_DIR / "fwi_run"
 
 
 def nvcc() -> str:
@@ -61,9 +65,22 @@ def build(force: bool = False, verbose_ptxas: bool = False, defines=(), out: Pat
         tmp = LIB.with_suffix(".so.tmp")
         _run([nvcc(), "-shared", *ARCH, "-o", str(tmp), *map(str, objs)])
         os.replace(tmp, LIB)
+    app_deps = [APP_DIR / "fwi_main.cpp", APP_DIR / "ini.hpp", ROOT / "include" / "fwi_psv.h", LIB]
+    if force or not APP.exists() or APP.stat().st_mtime < max(p.stat().st_mtime for p in app_deps):
+        build_app()
     if verbose_ptxas:
         print("\n".join(logs))
     return LIB
+
+
+def build_app() -> Path:
+    """The host driver: g++ against the C ABI, libfwi_psv.so found next to it."""
+    cxx = os.environ.get("CXX", "g++")
+    tmp = APP.with_suffix(".tmp")
+    _run([cxx, "-O2", "-std=c++17", f"-I{ROOT / 'include'}", f"-I{APP_DIR}", str(APP_DIR / "fwi_main.cpp"),
+          "-o", str(tmp), f"-L{OUT_DIR}", "-lfwi_psv", "-Wl,-rpath,$ORIGIN"])
+    os.replace(tmp, APP)
+    return APP
 
 
 def _build_variant(defines, out: Path) -> Path:

@@ -511,6 +511,9 @@ struct Engine {
     double pre_c[3] = {1.0, 1.0, 1.0};  // C_lam, C_mu, C_rho
     DBuf d_wmax;
     double out_scale(int q) const { return pre_on ? 1.0 / (pre_c[q] * pre_c[q]) : 1.0; }
+    // wavefield snapshots of the recording sweep (forward_kernel_PSV_GPU.cu:1067-1080)
+    int snap_interval = 0, snap_field = F_SZZ, nsnap = 0;
+    DBuf d_snapshots;  // [B][nsnap][field]
     HBuf h_stage, h_rec, h_grad;
     DBuf d_err;  // kernel error flags (bounded waits that timed out)
     bool obs_valid = false;
@@ -873,6 +876,8 @@ struct Engine {
         FWI_TRY(grow(d_blow, 16));
         FWI_TRY(grow(d_obsf, std::max<size_t>(1, (size_t)nrec) * nt * 4));
         FWI_TRY(grow(d_items_f, (size_t)cap * sizeof(ItemDesc)));
+        nsnap = snap_interval > 0 ? 1 + (nt - 1) / snap_interval : 0;
+        if (nsnap) FWI_TRY(grow(d_snapshots, (size_t)cap * nsnap * field * 4));
         FWI_TRY(grow(d_items_a, (size_t)cap * sizeof(ItemDesc)));
         Bcap = cap;
         B = nb;
@@ -1060,7 +1065,8 @@ struct Engine {
     std::string shape_key() const {
         return "|B" + std::to_string(B) + "|r" + std::to_string(rows.size()) + "|s" +
                std::to_string(slots) + "|st" + std::to_string(strategy) + "|t" + std::to_string(ntiles) +
-               "|g" + std::to_string(grad_on ? 1 : 0) + "|m" + std::to_string(grad_mode);
+               "|g" + std::to_string(grad_on ? 1 : 0) + "|m" + std::to_string(grad_mode) + "|sn" +
+               std::to_string(snap_interval) + "." + std::to_string(snap_field);
     }
 
     // FP64 host observed data -> resident FP32 rows [nrec][nt] for the given receivers.
@@ -1172,12 +1178,20 @@ struct Engine {
         return FWI_OK;
     }
 
-    // forward steps [t0, t1) of the working forward state
+    // forward steps [t0, t1) of the working forward state; the recording sweep
+    // also takes the snapshots (after the step, as the reference writes them)
     void forward_steps(int t0, int t1, bool record, bool store) {
         for (int it = t0; it < t1; it++) {
             unsigned sf = (store && it % fwi_dt == 0) ? FL_STORE : 0u;
             unsigned vf = FL_INJECT | (record ? (FL_RECORD | FL_WE) : 0u);
             step(false, it, sf, vf);
+            if (record && snap_interval > 0 && it % snap_interval == 0) {
+                const int k = it / snap_interval;
+                for (int b = 0; b < B; b++)
+                    cudaMemcpyAsync(d_snapshots.as<float>() + ((size_t)b * nsnap + k) * field,
+                                    d_fwd.as<float>() + (size_t)b * state + (size_t)snap_field * field,
+                                    field * 4, cudaMemcpyDeviceToDevice, stream);
+            }
         }
     }
     // adjoint steps t1-1 down to t0 (inclusive), gradient at sampled steps
@@ -1847,6 +1861,30 @@ int fwi_psv_set_model_lmr(fwi_psv_engine* h, const double* lam, const double* mu
     std::vector<double> mz(na), rz(na), rx(na);
     fwi::average_parameters(e.nzt, e.nxt, mu, rho, mz.data(), rz.data(), rx.data());
     return e.set_model(lam, mu, mz.data(), rz.data(), rx.data());
+}
+
+int fwi_psv_set_snapshots(fwi_psv_engine* h, int interval, int which) {
+    GUARD_ENGINE(h);
+    if (interval < 0 || which < 0 || which > 4) return fail(FWI_ERR_INVALID, "interval >= 0, field 0..4");
+    Engine& e = h->e;
+    e.snap_interval = interval;
+    e.snap_field = which;
+    e.invalidate_batch();
+    return FWI_OK;
+}
+
+int fwi_psv_snapshot(fwi_psv_engine* h, int slot, int k, double* out) {
+    GUARD_ENGINE(h);
+    Engine& e = h->e;
+    if (!out || slot < 0 || slot >= e.B || k < 0 || k >= e.nsnap || !e.d_snapshots.p)
+        return fail(FWI_ERR_INVALID, "no such snapshot (slot, index) of the last forward");
+    FWI_TRY(e.bind());
+    std::vector<float> hbuf(e.field);
+    CUDA_TRY(cudaMemcpy(hbuf.data(), e.d_snapshots.as<float>() + ((size_t)slot * e.nsnap + k) * e.field,
+                        e.field * 4, cudaMemcpyDeviceToHost));
+    for (int iz = 0; iz < e.nzt; iz++)
+        for (int ix = 0; ix < e.nxt; ix++) out[(size_t)iz * e.nxt + ix] = hbuf[(size_t)iz * e.pitch + ix];
+    return FWI_OK;
 }
 
 int fwi_psv_get_layout(fwi_psv_engine* h, fwi_psv_layout* o) {

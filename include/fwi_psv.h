@@ -239,6 +239,15 @@ int fwi_psv_time_kernels(fwi_psv_engine* e, int reps, double ms[4]);
  * rounding differs between mappings. */
 int fwi_psv_set_exec(fwi_psv_engine* e, int use_graphs, int block_x, int tile_z, int batch);
 
+/* Wavefield snapshots of the recording forward sweep (forward_kernel_PSV_GPU.cu
+ * :1067-1080): field `which` (0 vx, 1 vz, 2 sxx, 3 szx, 4 szz; the reference
+ * writes szz) of every batch slot after each time step it with
+ * it % interval == 0.  interval 0 switches them off. */
+int fwi_psv_set_snapshots(fwi_psv_engine* e, int interval, int which);
+/* Snapshot k (time step k * interval) of batch slot `slot` of the last
+ * forward, [nzt][nxt]. */
+int fwi_psv_snapshot(fwi_psv_engine* e, int slot, int k, double* out);
+
 /* Grid and FWI-window extents of an engine (after fwi_psv_set_fwi). */
 typedef struct fwi_psv_layout {
     int nt, nzt, nxt, fpad, ppad, npml, fsurf, fdorder;
