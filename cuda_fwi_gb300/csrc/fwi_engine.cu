@@ -98,8 +98,9 @@ __global__ void events_kernel(const ItemDesc* __restrict__ items, int it, unsign
             if (e > e0 && D.ev_x[e - 1] == x && D.ev[e - 1].x == v.x) continue;  // not the cell's first
             float* c = D.vz + (size_t)v.x * P + x;
             float val = *c;
+            const bool undo = (flags & FL_REVERSE) != 0;  // remove the injection of step it
             for (int q = e; q < e1 && D.ev_x[q] == x && D.ev[q].x == v.x && D.ev[q].y >= 0; q++)
-                val += D.inj[(size_t)D.ev[q].y * nt + it];
+                val = undo ? val - D.inj[(size_t)D.ev[q].y * nt + it] : val + D.inj[(size_t)D.ev[q].y * nt + it];
             *c = val;
         }
     __syncthreads();
@@ -141,6 +142,46 @@ __global__ void materials_kernel(const double* __restrict__ lam, const double* _
         mat[2 * field + o] = mz;
         mat[3 * field + o] = bx;
         mat[4 * field + o] = bz;
+    }
+}
+
+// Random-boundary frame (Clapp's random boundaries for reverse-time
+// reconstruction, SEG 2009): copy the materials and, in the padding around the
+// model, scale the velocities by f = 1 - alpha (d / ppad) u, with d the depth
+// into the padding and u a hashed uniform number in [0, 1) per cell, i.e.
+// L, M2, MZX by f^2 with density unchanged.  Velocities only decrease, so the
+// time step stays stable; the frame scatters boundary reflections instead of
+// absorbing them, which keeps the scheme reversible (no damping).
+__device__ __forceinline__ unsigned hash_u32(unsigned x) {
+    x ^= x >> 16;
+    x *= 0x7feb352du;
+    x ^= x >> 15;
+    x *= 0x846ca68bu;
+    x ^= x >> 16;
+    return x;
+}
+__global__ void random_frame_kernel(const float* __restrict__ mat, float* __restrict__ rb, size_t field, int nzt,
+                                    int nxt, int pitch, int ppad, int fsurf, unsigned seed, float alpha) {
+    const size_t n = (size_t)nzt * nxt;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const int iz = (int)(i / nxt), ix = (int)(i % nxt);
+        int d = 0;
+        d = max(d, ppad - ix);
+        d = max(d, ix - (nxt - 1 - ppad));
+        if (!fsurf) d = max(d, ppad - iz);
+        d = max(d, iz - (nzt - 1 - ppad));
+        float f2 = 1.f;
+        if (d > 0 && ppad > 0) {
+            const float u = (float)(hash_u32((unsigned)i * 2654435761u + seed) >> 8) * (1.f / 16777216.f);
+            const float f = 1.f - alpha * ((float)d / (float)ppad) * u;
+            f2 = f * f;
+        }
+        const size_t o = (size_t)iz * pitch + ix;
+        rb[o] = mat[o] * f2;
+        rb[field + o] = mat[field + o] * f2;
+        rb[2 * field + o] = mat[2 * field + o] * f2;
+        rb[3 * field + o] = mat[3 * field + o];
+        rb[4 * field + o] = mat[4 * field + o];
     }
 }
 
@@ -514,6 +555,12 @@ struct Engine {
     // wavefield snapshots of the recording sweep (forward_kernel_PSV_GPU.cu:1067-1080)
     int snap_interval = 0, snap_field = F_SZZ, nsnap = 0;
     DBuf d_snapshots;  // [B][nsnap][field]
+    // random-boundary strategy: frame materials, their validity, whether the
+    // current batch's forward items use them
+    DBuf d_mat_rb;
+    bool rb_valid = false, rb_active = false;
+    unsigned rb_seed = 20090625u;
+    float rb_alpha = 0.5f;
     HBuf h_stage, h_rec, h_grad;
     DBuf d_err;  // kernel error flags (bounded waits that timed out)
     bool obs_valid = false;
@@ -613,6 +660,9 @@ struct Engine {
     // The exact adjoint always runs the checkpointed schedule, one time step per unit.
     bool exact() const { return grad_mode == FWI_GRAD_EXACT; }
     bool ckpt_mode() const { return strategy == FWI_STORE_BINOMIAL || exact(); }
+    bool store_mode() const { return strategy == FWI_STORE_FULL && !exact(); }
+    bool random_mode() const { return strategy == FWI_STORE_RANDOM && !exact(); }
+    bool state_source() const { return ckpt_mode() || random_mode(); }  // gradient reads the forward state
     int unit() const { return exact() ? 1 : fwi_dt; }
     int nunits() const { return exact() ? nt : nft; }
 
@@ -654,6 +704,7 @@ struct Engine {
                                  stream));
         CUDA_TRY(cudaStreamSynchronize(stream));
         have_model = true;
+        rb_valid = false;
         return FWI_OK;
     }
 
@@ -675,6 +726,7 @@ struct Engine {
         CUDA_TRY(cudaStreamSynchronize(stream));
         zero_mu = z != 0;
         have_model = true;
+        rb_valid = false;
         return FWI_OK;
     }
 
@@ -860,7 +912,21 @@ struct Engine {
         FWI_TRY(grow(d_grad, (size_t)cap * 3 * nf * 4));
         FWI_TRY(grow(d_gsum, (size_t)3 * nf * 4));
         FWI_TRY(grow(d_gacc, (size_t)3 * nf * 4));
-        if (keep && !ckpt_mode()) FWI_TRY(grow(d_store, (size_t)cap * nft * 5 * nf * 4));
+        if (keep && store_mode()) FWI_TRY(grow(d_store, (size_t)cap * nft * 5 * nf * 4));
+        rb_active = keep && random_mode();
+        if (rb_active && !rb_valid) {
+            if (fsurf) return fail(FWI_ERR_UNSUPPORTED, "random boundaries need the model without a free surface");
+            if (kmap != 3)
+                return fail(FWI_ERR_UNSUPPORTED, "random-boundary reconstruction runs on the TMA mapping only");
+            FWI_TRY(d_mat_rb.ensure(5 * field * sizeof(float)));
+            drop_graphs();
+            CUDA_TRY(cudaMemsetAsync(d_mat_rb.p, 0, 5 * field * sizeof(float), stream));
+            const size_t n = (size_t)nzt * nxt;
+            random_frame_kernel<<<(int)std::min<size_t>((n + 255) / 256, (size_t)num_sms * 8), 256, 0, stream>>>(
+                d_mat.as<float>(), d_mat_rb.as<float>(), field, nzt, nxt, pitch, ppad, fsurf, rb_seed, rb_alpha);
+            CUDA_TRY(cudaGetLastError());
+            rb_valid = true;
+        }
         if (keep && ckpt_mode() && want_slots > 0) FWI_TRY(grow(d_snap, (size_t)want_slots * cap * state * 4));
         if (exact()) {
             FWI_TRY(grow(d_nxt, (size_t)cap * state * 4));
@@ -982,12 +1048,12 @@ struct Engine {
         const int hx = (FPv + 3) / 4 * 4;
         const int wx = kTmaTX + 2 * hx, wz = kTmaTZ + 2 * FPv;
         const size_t rb = (size_t)pitch * 4, sb = state * 4;
-        const float* mat = d_mat.as<float>();
         float* bases[3] = {d_fwd.as<float>(), d_adj.as<float>(), d_nxt.p ? d_nxt.as<float>() : nullptr};
         float* webase[3] = {d_ws.as<float>(), d_wr.as<float>(), d_ws.as<float>()};
         for (int w = 0; w < 3; w++) {
             float* st = bases[w];
             if (!st) continue;
+            const float* mat = (w == 0 && rb_active) ? d_mat_rb.as<float>() : d_mat.as<float>();
             StressMaps& S = smaps[w];
             FWI_TRY(make_map(&S.vx, st + F_VX * field, nxt, nzt, Bcap, rb, sb, wx, wz));
             FWI_TRY(make_map(&S.vz, st + F_VZ * field, nxt, nzt, Bcap, rb, sb, wx, wz));
@@ -1009,6 +1075,7 @@ struct Engine {
         }
         {
             // adjoint stress pass (128 x 8 tiles): adjoint state, ux/uz, forward state
+            const float* mat = d_mat.as<float>();
             const int wza = kAdjTZ + 2 * FPv;
             float* a = d_adj.as<float>();
             float* f = d_fwd.as<float>();
@@ -1065,7 +1132,8 @@ struct Engine {
     std::string shape_key() const {
         return "|B" + std::to_string(B) + "|r" + std::to_string(rows.size()) + "|s" +
                std::to_string(slots) + "|st" + std::to_string(strategy) + "|t" + std::to_string(ntiles) +
-               "|g" + std::to_string(grad_on ? 1 : 0) + "|m" + std::to_string(grad_mode) + "|sn" +
+               "|g" + std::to_string(grad_on ? 1 : 0) + "|m" + std::to_string(grad_mode) + "|rb" +
+               std::to_string(rb_active ? 1 : 0) + "|sn" +
                std::to_string(snap_interval) + "." + std::to_string(snap_field);
     }
 
@@ -1116,7 +1184,10 @@ struct Engine {
             d.hz[k] = k < fpad ? (float)((1.0 / dz) * hc[k + 1]) : 0.f;
         }
         d.cpml = d_cpml.as<float>();
-        const float* m = d_mat.as<float>();
+        // the random-boundary forward: frame materials, no CPML
+        const bool rbf = rb_active && !adj && state_base == nullptr;
+        if (rbf) d.npml = 0;
+        const float* m = rbf ? d_mat_rb.as<float>() : d_mat.as<float>();
         d.L = m; d.M2 = m + field; d.MZX = m + 2 * field; d.BX = m + 3 * field; d.BZ = m + 4 * field;
         float* st = (state_base ? state_base : adj ? d_adj.as<float>() : d_fwd.as<float>()) + (size_t)b * state;
         d.vx = st + F_VX * field; d.vz = st + F_VZ * field; d.sxx = st + F_SXX * field;
@@ -1138,7 +1209,7 @@ struct Engine {
             d.glam = d_grad.as<float>() + (size_t)b * 3 * nf;
             d.gmu = d.glam + nf;
             d.grho = d.gmu + nf;
-            if (ckpt_mode()) {
+            if (state_source()) {
                 d.fwd_kind = 1;
                 d.fwd = d_fwd.as<float>() + (size_t)b * state;
                 d.fwd_fs = (long long)field;
@@ -1153,7 +1224,7 @@ struct Engine {
     // Adjoint stress pass with the reference gradient; the TMA kernel reads the
     // forward fields from the checkpointed working state (fwd_kind 1).
     void pass_stress_adj(const ItemDesc* items, int it, unsigned flags) {
-        if (kmap == 3 && ckpt_mode())
+        if (kmap == 3 && state_source())
             tset.adjoint(dim3(grid_tma_a), stream, amap, items, tgrid_a, it, flags, d_err.as<int>());
         else
             ks.stress_a(dim3(grid_sa), stream, items, d_tiles_p, ntiles, it, flags, d_err.as<int>());
@@ -1277,7 +1348,7 @@ struct Engine {
         CUDA_TRY(cudaEventCreate(&e1));
         launches_now = 0;
         CUDA_TRY(cudaEventRecord(e0, stream));
-        const bool store = keep && !ckpt_mode();
+        const bool store = keep && store_mode();
         const bool ckpt = keep && ckpt_mode();
         // checkpoint positions of the first sweep: the SAVE actions before the first ADJOINT
         std::vector<std::pair<int, int>> saves;  // (state, slot)
@@ -1359,7 +1430,7 @@ struct Engine {
         CUDA_TRY(cudaEventCreate(&b));
         const ItemDesc* itf = d_items_f.as<ItemDesc>();
         const ItemDesc* ita = d_items_a.as<ItemDesc>();
-        const bool have_adj_src = ckpt_mode() ? true : d_store.p != nullptr;
+        const bool have_adj_src = state_source() ? true : d_store.p != nullptr;
         for (int k = 0; k < 4; k++) {
             const bool adj = k >= 2;
             if (adj && !have_adj_src) { ms[k] = 0.0; continue; }
@@ -1394,8 +1465,10 @@ struct Engine {
         FWI_TRY(bind());
         if (!fwd_kept) return fail(FWI_ERR_NOFORWARD, "backward needs a forward(keep=1)");
         if (!have_resid) return fail(FWI_ERR_STATE, "backward needs observed data (forward obs) or a loaded residual");
-        if (bwd_done && ckpt_mode())
+        if (bwd_done && state_source())
             return fail(FWI_ERR_STATE, "the checkpointed forward was consumed by the previous backward");
+        if (random_mode() && !rb_active)
+            return fail(FWI_ERR_STATE, "the forward was not run with random boundaries");
         if (exact() && zero_mu)
             return fail(FWI_ERR_UNSUPPORTED, "the exact adjoint needs mu > 0 on every interior cell");
         cudaEvent_t e0, e1;
@@ -1404,7 +1477,7 @@ struct Engine {
         launches_now = 0;
         long long recompute = 0;
         CUDA_TRY(cudaEventRecord(e0, stream));
-        const std::string key = std::string(ckpt_mode() ? "bwdC" : "bwdS") + shape_key();
+        const std::string key = std::string(ckpt_mode() ? "bwdC" : random_mode() ? "bwdR" : "bwdS") + shape_key();
         FWI_TRY(run_phase(key, [&]() -> int {
             CUDA_TRY(cudaMemsetAsync(d_adj.p, 0, (size_t)B * state * 4, stream));
             CUDA_TRY(cudaMemsetAsync(d_wr.p, 0, (size_t)B * field * 4, stream));
@@ -1412,6 +1485,21 @@ struct Engine {
             CUDA_TRY(cudaMemsetAsync(d_uz.p, 0, (size_t)B * field * 4, stream));
             CUDA_TRY(cudaMemsetAsync(d_grad.p, 0, (size_t)B * 3 * nf * 4, stream));
             if (exact()) CUDA_TRY(cudaMemsetAsync(d_exact.p, 0, (size_t)B * 9 * field * 4, stream));
+            if (random_mode()) {
+                // reverse-time reconstruction of the source wavefield, one step
+                // ahead of the adjoint step that correlates with it
+                const ItemDesc* itf = d_items_f.as<ItemDesc>();
+                for (int it = nt - 1; it >= 0; it--) {
+                    events_kernel<<<B, 256, 0, stream>>>(itf, it, FL_INJECT | FL_REVERSE);
+                    pass_velocity(0, itf, it, FL_REVERSE);
+                    pass_stress_fwd(0, itf, it, FL_REVERSE);
+                    launches_now += 3;
+                    const unsigned sf = (grad_on && it % fwi_dt == 0) ? FL_GRAD : 0u;
+                    step(true, it, sf, FL_INJECT | FL_WE);
+                }
+                recompute += nt;
+                return FWI_OK;
+            }
             if (!ckpt_mode()) {
                 adjoint_steps(0, nt);
                 return FWI_OK;
@@ -1500,7 +1588,9 @@ struct Engine {
         stats.last_backward_ms = ms;
         stats.launches = launches_now;
         stats.adjoint_steps = nt;
-        stats.recompute_steps = ckpt_mode() ? (recompute > 0 ? recompute : plan_cost) * unit() : 0;
+        stats.recompute_steps = ckpt_mode()     ? (recompute > 0 ? recompute : plan_cost) * unit()
+                                : random_mode() ? (int64_t)nt
+                                                : 0;
         const double k0 = out_scale(0), k1 = out_scale(1), k2 = out_scale(2);
         for (size_t s = 0; s < ntrip && want; s++)
             for (size_t i = 0; i < nf; i++) {
@@ -1940,8 +2030,6 @@ int fwi_psv_set_strategy(fwi_psv_engine* h, int strategy, int snapshots, size_t 
     GUARD_ENGINE(h);
     if (strategy != FWI_STORE_FULL && strategy != FWI_STORE_BINOMIAL && strategy != FWI_STORE_RANDOM)
         return fail(FWI_ERR_INVALID, "unknown strategy");
-    if (strategy == FWI_STORE_RANDOM)
-        return fail(FWI_ERR_UNSUPPORTED, "random-boundary reconstruction is not available in this build");
     if (snapshots < 0) return fail(FWI_ERR_INVALID, "snapshots must be >= 0");
     Engine& e = h->e;
     e.strategy = strategy;

@@ -51,6 +51,7 @@ enum Flags : unsigned {
     FL_WE = 1u << 2,      // accumulate the energy sum We += vx^2 + vz^2
     FL_INJECT = 1u << 3,  // add the injection signal at source positions
     FL_RECORD = 1u << 4,  // record vz at receiver positions
+    FL_REVERSE = 1u << 5, // undo a step: subtract the increments / the injection (TMA mapping)
 };
 
 struct __align__(16) ItemDesc {

@@ -244,6 +244,9 @@ __device__ __forceinline__ void stress_compute(const ItemDesc& D, const float* s
     int xf = -1;
     if ((flags & FL_STORE) && D.store && ix >= D.wx1 && ix < D.wx2 && (ix - D.wx1) % D.fwi_dx == 0)
         xf = (ix - D.wx1) / D.fwi_dx;
+    // FL_REVERSE undoes the step (s^n = s^{n+1} - S(v^n)); used only without
+    // CPML and free surface, where the update is a pure increment
+    const float sg = (flags & FL_REVERSE) ? -1.f : 1.f;
 #pragma unroll
     for (int rr = 0; rr < R; rr++) {
         const int r = r0 + rr;
@@ -293,10 +296,10 @@ __device__ __forceinline__ void stress_compute(const ItemDesc& D, const float* s
             s[F_SZX * fs] = szx;
             s[F_SZZ * fs] = szz;
         }
-        szx += MZ * (vz_x + vx_z);
+        szx += sg * (MZ * (vz_x + vx_z));
         const float tr = L * (vx_x + vz_z);
-        sxx += tr + M2 * vx_x;
-        szz += tr + M2 * vz_z;
+        sxx += sg * (tr + M2 * vx_x);
+        szz += sg * (tr + M2 * vz_z);
         if (fsurf && iz == FP) {
             szz = 0.f;
             szx = 0.f;
@@ -407,6 +410,7 @@ __device__ __forceinline__ void velocity_compute(const ItemDesc& D, const float*
         }
     }
     const bool we = (flags & FL_WE) != 0;
+    const float sg = (flags & FL_REVERSE) ? -1.f : 1.f;  // v^n = v^{n+1} - V(s^{n+1})
 #pragma unroll
     for (int rr = 0; rr < R; rr++) {
         const int r = r0 + rr;
@@ -443,8 +447,8 @@ __device__ __forceinline__ void velocity_compute(const ItemDesc& D, const float*
             szx_z = szx_z * cz.iKh + m2;
         }
         const int ci = r * kTmaTX + tx;
-        const float vxn = cen[2 * G::CEN + ci] + cen[ci] * (sxx_x + szx_z);
-        const float vzn = cen[3 * G::CEN + ci] + cen[G::CEN + ci] * (szx_x + szz_z);
+        const float vxn = cen[2 * G::CEN + ci] + sg * (cen[ci] * (sxx_x + szx_z));
+        const float vzn = cen[3 * G::CEN + ci] + sg * (cen[G::CEN + ci] * (szx_x + szz_z));
         const size_t c = (size_t)iz * P + ix;
         if (we) gwe[c] = cen[4 * G::CEN + ci] + (vxn * vxn + vzn * vzn);
         gvx[c] = vxn;

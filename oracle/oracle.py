@@ -129,7 +129,7 @@ def total_grid(nx, nz, fdorder, npml, fsurf):
 class _Ctx:
     """Keeps the numpy buffers behind the ctypes structs alive."""
 
-    def __init__(self, p, lam=None, mu=None, rho=None):
+    def __init__(self, p, lam=None, mu=None, rho=None, averaged=None):
         self.p = p
         self.cp = {k: np.ascontiguousarray(v, np.float64) for k, v in p.cpml.items()}
         g = Grid()
@@ -144,7 +144,8 @@ class _Ctx:
         lam = p.lam if lam is None else lam
         mu = p.mu if mu is None else mu
         rho = p.rho if rho is None else rho
-        self.mat = [np.ascontiguousarray(x, np.float64) for x in (lam, mu)] + average(lam, mu, rho)
+        avg = average(lam, mu, rho) if averaged is None else [np.ascontiguousarray(a, np.float64) for a in averaged]
+        self.mat = [np.ascontiguousarray(x, np.float64) for x in (lam, mu)] + avg
         m = Medium()
         for k, a in zip(("lam", "mu", "mu_zx", "rho_zp", "rho_xp"), self.mat):
             setattr(m, k, _d(a))
@@ -182,10 +183,11 @@ class _Ctx:
         return f, store
 
 
-def forward(p, shot=0, fwinv=False, lam=None, mu=None, rho=None):
+def forward(p, shot=0, fwinv=False, lam=None, mu=None, rho=None, averaged=None):
     """orc_forward for one shot.  Returns dict(rec [nrec][nt], wave fields, We,
-    CPML memory, store (5 arrays [nft][nfz][nfx]) when fwinv)."""
-    ctx = _Ctx(p, lam, mu, rho)
+    CPML memory, store (5 arrays [nft][nfz][nfx]) when fwinv).  `averaged` =
+    (mu_zx, rho_zp, rho_xp) replaces the averages of lam/mu/rho."""
+    ctx = _Ctx(p, lam, mu, rho, averaged)
     src, keep1 = ctx.seis(p.src_x, p.src_z, p.src_comp, p.src_shot)
     rec, keep2 = ctx.seis(p.rec_x, p.rec_z, p.rec_comp, p.rec_shot)
     sig = np.ascontiguousarray(p.src_signal, np.float64) if p.nsrc else np.zeros((1, p.nt))

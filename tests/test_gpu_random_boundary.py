@@ -1,0 +1,85 @@
+"""Random-boundary reconstruction (FWI_STORE_RANDOM) against the FP64 oracle.
+
+The engine rebuilds the random-boundary forward wavefield backwards in time;
+the oracle computes the reference gradient from the stored wavefield of the
+same forward (oracle/random_boundary.py).  The difference is the FP32
+time-reversal drift plus FP32 arithmetic.
+"""
+import numpy as np
+import pytest
+
+from conftest import rel_l2
+from cuda_fwi_gb300 import _capi
+from cuda_fwi_gb300 import problem as P
+from cuda_fwi_gb300.engine import Engine
+from oracle import oracle as O
+from oracle import random_boundary as RB
+
+pytestmark = pytest.mark.gpu
+
+
+def _case(order, nshots=1, nt=220, fwi=(1, 1, 1)):
+    kw = dict(fdorder=order, nx=56, nz=40, nt=nt, npml=10, nshots=nshots, nrec=7, perturb=0.05, fwi=fwi)
+    p = P.small(seed=5, **kw)
+    t = P.small(seed=15, **kw)
+    obs = np.zeros((p.nrec, p.nt))
+    for s in range(nshots):
+        rows = O.shot_rows(t, s)
+        obs[rows] = O.forward(t, s)["rec"][rows]
+    return p, obs
+
+
+@pytest.mark.parametrize("order,fwi", [(2, (1, 1, 1)), (4, (2, 1, 1)), (8, (1, 2, 2))])
+def test_random_boundary_matches_oracle(order, fwi):
+    p, obs = _case(order, fwi=fwi)
+    J, g_o = RB.gradient(p, obs, 0)
+    with Engine(p) as eng:
+        eng.set_strategy("random")
+        rec, mis = eng.forward([0], obs, keep=True)
+        g = eng.backward()
+        st = eng.stats()
+    assert mis[0] == pytest.approx(J, rel=1e-4)
+    for i in range(3):
+        assert rel_l2(g[i][0], g_o[i]) <= 1e-3, i
+    assert st["recompute_steps"] == p.nt
+
+
+def test_random_boundary_batched_gradient_and_cost():
+    p, obs = _case(8, nshots=3)
+    ref = [np.zeros((p.nfz, p.nfx)) for _ in range(3)]
+    for s in range(3):
+        _, g = RB.gradient(p, obs, s)
+        for i in range(3):
+            ref[i] += g[i]
+    with Engine(p) as eng:
+        eng.set_strategy("random")
+        g, mis = eng.gradient([0, 1, 2], obs)
+        st = eng.stats()
+        # the CPML gradient of the same shots: same structure, different boundary model
+        eng.set_strategy("binomial", snapshots=8)
+        gb, _ = eng.gradient([0, 1, 2], obs)
+    for i in range(3):
+        assert rel_l2(g[i], ref[i]) <= 1e-3, i
+    assert st["device_bytes"] > 0
+    # interior agreement with the absorbing-boundary gradient (not equal: the
+    # random frame scatters instead of absorbing)
+    z = slice(p.ppad, p.nzt - p.ppad)
+    x = slice(p.ppad, p.nxt - p.ppad)
+    c = np.corrcoef(g[0][z, x].ravel(), gb[0][z, x].ravel())[0, 1]
+    assert c > 0.5
+
+
+def test_random_boundary_refusals():
+    p, obs = _case(4, nt=40)
+    with Engine(p) as eng:
+        eng.set_strategy("random")
+        eng.set_exec(True, 64, 0)  # vectorised cells: no reverse step there
+        with pytest.raises(_capi.FwiError) as e:
+            eng.forward([0], obs, keep=True)
+        assert e.value.code == "FWI_ERR_UNSUPPORTED"
+    q = P.small(fdorder=4, nx=40, nz=30, nt=40, npml=6, fsurf=1, nrec=4)
+    with Engine(q) as eng:
+        eng.set_strategy("random")
+        with pytest.raises(_capi.FwiError) as e:
+            eng.forward([0], np.zeros((q.nrec, q.nt)), keep=True)
+        assert e.value.code == "FWI_ERR_UNSUPPORTED"
