@@ -539,10 +539,11 @@ struct Engine {
     // exact discrete adjoint: forward state n+1, derivative adjoints + sensitivities, descriptors
     DBuf d_nxt, d_exact, d_exd, d_items_n;
     ExactSet xs{};
-    // TMA mapping: kernels, tensor maps per state buffer (0 fwd, 1 adj, 2 state n+1), tile grid
+    // TMA mapping: kernels, tensor maps per state buffer (0 fwd, 1 adj, 2 state n+1,
+    // 3 fwd with the random-boundary materials), tile grid
     TmaSet tset{};
-    StressMaps smaps[3];
-    VelMaps vmaps[3];
+    StressMaps smaps[4];
+    VelMaps vmaps[4];
     AdjMaps amap;
     TmaGrid tgrid{}, tgrid_a{};
     int grid_tma = 1, grid_tma_a = 1;
@@ -557,7 +558,7 @@ struct Engine {
     DBuf d_snapshots;  // [B][nsnap][field]
     // random-boundary strategy: frame materials, their validity, whether the
     // current batch's forward items use them
-    DBuf d_mat_rb;
+    DBuf d_mat_rb, d_items_rb;
     bool rb_valid = false, rb_active = false;
     unsigned rb_seed = 20090625u;
     float rb_alpha = 0.5f;
@@ -942,6 +943,7 @@ struct Engine {
         FWI_TRY(grow(d_blow, 16));
         FWI_TRY(grow(d_obsf, std::max<size_t>(1, (size_t)nrec) * nt * 4));
         FWI_TRY(grow(d_items_f, (size_t)cap * sizeof(ItemDesc)));
+        if (keep && random_mode()) FWI_TRY(grow(d_items_rb, (size_t)cap * sizeof(ItemDesc)));
         nsnap = snap_interval > 0 ? 1 + (nt - 1) / snap_interval : 0;
         if (nsnap) FWI_TRY(grow(d_snapshots, (size_t)cap * nsnap * field * 4));
         FWI_TRY(grow(d_items_a, (size_t)cap * sizeof(ItemDesc)));
@@ -1011,11 +1013,12 @@ struct Engine {
             CUDA_TRY(cudaMemcpyAsync(d_ev_a.p, eva.data(), eva.size() * 8, cudaMemcpyHostToDevice, stream));
         if (nrows)
             CUDA_TRY(cudaMemcpyAsync(d_rowrec.p, rows.data(), nrows * 4, cudaMemcpyHostToDevice, stream));
-        std::vector<ItemDesc> itf(B), ita(B), itn(B);
+        std::vector<ItemDesc> itf(B), ita(B), itn(B), itr(B);
         std::vector<ExactDesc> exd(B);
         for (int b = 0; b < B; b++) {
             fill_item(itf[b], b, false);
             fill_item(ita[b], b, true);
+            if (rb_active) fill_item(itr[b], b, false, nullptr, true);
             if (exact()) {
                 fill_item(itn[b], b, false, d_nxt.as<float>());
                 ExactDesc& x = exd[b];
@@ -1030,6 +1033,8 @@ struct Engine {
         }
         CUDA_TRY(cudaMemcpyAsync(d_items_f.p, itf.data(), B * sizeof(ItemDesc), cudaMemcpyHostToDevice, stream));
         CUDA_TRY(cudaMemcpyAsync(d_items_a.p, ita.data(), B * sizeof(ItemDesc), cudaMemcpyHostToDevice, stream));
+        if (rb_active)
+            CUDA_TRY(cudaMemcpyAsync(d_items_rb.p, itr.data(), B * sizeof(ItemDesc), cudaMemcpyHostToDevice, stream));
         if (exact()) {
             CUDA_TRY(cudaMemcpyAsync(d_items_n.p, itn.data(), B * sizeof(ItemDesc), cudaMemcpyHostToDevice, stream));
             CUDA_TRY(cudaMemcpyAsync(d_exd.p, exd.data(), B * sizeof(ExactDesc), cudaMemcpyHostToDevice, stream));
@@ -1048,12 +1053,13 @@ struct Engine {
         const int hx = (FPv + 3) / 4 * 4;
         const int wx = kTmaTX + 2 * hx, wz = kTmaTZ + 2 * FPv;
         const size_t rb = (size_t)pitch * 4, sb = state * 4;
-        float* bases[3] = {d_fwd.as<float>(), d_adj.as<float>(), d_nxt.p ? d_nxt.as<float>() : nullptr};
-        float* webase[3] = {d_ws.as<float>(), d_wr.as<float>(), d_ws.as<float>()};
-        for (int w = 0; w < 3; w++) {
+        float* bases[4] = {d_fwd.as<float>(), d_adj.as<float>(), d_nxt.p ? d_nxt.as<float>() : nullptr,
+                           rb_active ? d_fwd.as<float>() : nullptr};
+        float* webase[4] = {d_ws.as<float>(), d_wr.as<float>(), d_ws.as<float>(), d_ws.as<float>()};
+        for (int w = 0; w < 4; w++) {
             float* st = bases[w];
             if (!st) continue;
-            const float* mat = (w == 0 && rb_active) ? d_mat_rb.as<float>() : d_mat.as<float>();
+            const float* mat = w == 3 ? d_mat_rb.as<float>() : d_mat.as<float>();
             StressMaps& S = smaps[w];
             FWI_TRY(make_map(&S.vx, st + F_VX * field, nxt, nzt, Bcap, rb, sb, wx, wz));
             FWI_TRY(make_map(&S.vz, st + F_VZ * field, nxt, nzt, Bcap, rb, sb, wx, wz));
@@ -1169,7 +1175,7 @@ struct Engine {
         return t;
     }
 
-    void fill_item(ItemDesc& d, int b, bool adj, float* state_base = nullptr) {
+    void fill_item(ItemDesc& d, int b, bool adj, float* state_base = nullptr, bool rbf = false) {
         std::memset(&d, 0, sizeof d);
         d.nzt = nzt; d.nxt = nxt; d.pitch = pitch; d.fpad = fpad;
         d.ppad = ppad; d.npml = npml; d.tp = tp; d.pnx = pnx;
@@ -1185,7 +1191,6 @@ struct Engine {
         }
         d.cpml = d_cpml.as<float>();
         // the random-boundary forward: frame materials, no CPML
-        const bool rbf = rb_active && !adj && state_base == nullptr;
         if (rbf) d.npml = 0;
         const float* m = rbf ? d_mat_rb.as<float>() : d_mat.as<float>();
         d.L = m; d.M2 = m + field; d.MZX = m + 2 * field; d.BX = m + 3 * field; d.BZ = m + 4 * field;
@@ -1370,6 +1375,18 @@ struct Engine {
                 FWI_TRY(state_copy(snap(sv.second), d_fwd.as<float>()));
             }
             forward_steps(t, nt, true, store);
+            if (rb_active) {
+                // the random-boundary forward, from rest, for the backward's
+                // reconstruction (the recording sweep above keeps the CPML, so
+                // seismograms and residuals are the absorbing-boundary ones)
+                CUDA_TRY(cudaMemsetAsync(d_fwd.p, 0, (size_t)B * state * 4, stream));
+                const ItemDesc* itr = d_items_rb.as<ItemDesc>();
+                for (int it = 0; it < nt; it++) {
+                    pass_stress_fwd(3, itr, it, 0u);
+                    pass_velocity(3, itr, it, FL_INJECT);
+                    launches_now += 2;
+                }
+            }
             if (obs && nrows) {
                 CUDA_TRY(cudaMemsetAsync(d_blow.p, 0, 4, stream));
                 residual_kernel<<<(unsigned)nrows, 256, 0, stream>>>(
@@ -1488,11 +1505,11 @@ struct Engine {
             if (random_mode()) {
                 // reverse-time reconstruction of the source wavefield, one step
                 // ahead of the adjoint step that correlates with it
-                const ItemDesc* itf = d_items_f.as<ItemDesc>();
+                const ItemDesc* itr = d_items_rb.as<ItemDesc>();
                 for (int it = nt - 1; it >= 0; it--) {
-                    events_kernel<<<B, 256, 0, stream>>>(itf, it, FL_INJECT | FL_REVERSE);
-                    pass_velocity(0, itf, it, FL_REVERSE);
-                    pass_stress_fwd(0, itf, it, FL_REVERSE);
+                    events_kernel<<<B, 256, 0, stream>>>(itr, it, FL_INJECT | FL_REVERSE);
+                    pass_velocity(3, itr, it, FL_REVERSE);
+                    pass_stress_fwd(3, itr, it, FL_REVERSE);
                     launches_now += 3;
                     const unsigned sf = (grad_on && it % fwi_dt == 0) ? FL_GRAD : 0u;
                     step(true, it, sf, FL_INJECT | FL_WE);
@@ -1589,7 +1606,7 @@ struct Engine {
         stats.launches = launches_now;
         stats.adjoint_steps = nt;
         stats.recompute_steps = ckpt_mode()     ? (recompute > 0 ? recompute : plan_cost) * unit()
-                                : random_mode() ? (int64_t)nt
+                                : random_mode() ? (int64_t)2 * nt
                                                 : 0;
         const double k0 = out_scale(0), k1 = out_scale(1), k2 = out_scale(2);
         for (size_t s = 0; s < ntrip && want; s++)

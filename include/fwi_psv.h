@@ -103,16 +103,17 @@ enum {
     FWI_STORE_BINOMIAL = 1, /* binomial checkpointing with forward recompute */
     FWI_STORE_RANDOM = 2    /* random-boundary wavefield reconstruction (no CPML on the source side) */
 };
-/* FWI_STORE_RANDOM keeps one state per shot.  The recording forward runs
- * without CPML in a seeded random-velocity frame filling the padding
- * (velocities scaled by 1 - 0.5 (depth into the padding / ppad) u, u uniform
- * in [0, 1)), so its seismograms and misfit are those of that model; the
- * backward rebuilds the source wavefield by undoing the forward steps in
- * reverse (FP32 round-off makes it drift slightly from the recorded one) and
- * correlates it with the adjoint wavefield, which keeps the CPML.  Cost per
- * shot gradient: 3 nt time steps.  Needs the TMA mapping (the default), no
- * free surface (its surface row is assigned, not incremented, so it cannot be
- * undone) and FWI_GRAD_REFERENCE (FWI_GRAD_EXACT always checkpoints). */
+/* FWI_STORE_RANDOM keeps one state per shot.  The recording forward keeps
+ * the CPML (seismograms, misfit and residual as with the other strategies);
+ * a second forward runs without CPML in a seeded random-velocity frame filling
+ * the padding (velocities scaled by 1 - 0.5 (depth into the padding / ppad) u,
+ * u uniform in [0, 1)); the backward rebuilds that second wavefield by undoing
+ * its steps in reverse (FP32 round-off makes it drift slightly) and correlates
+ * it with the adjoint wavefield, which keeps the CPML.  Cost per shot
+ * gradient: 4 nt time steps (the frame forward and the reverse sweep count as
+ * recompute_steps).  Needs the TMA mapping (the default), no free surface (its
+ * surface row is assigned, not incremented, so it cannot be undone) and
+ * FWI_GRAD_REFERENCE (FWI_GRAD_EXACT always checkpoints). */
 
 /* Gradient formula.
  * FWI_GRAD_EXACT has no reference counterpart: it is dJ/d(lam, mu, rho) of

@@ -2,13 +2,16 @@
 
 TEST INFRASTRUCTURE ONLY: the checker of the engine's FWI_STORE_RANDOM.
 
-The engine's random-boundary strategy runs the recording forward without
+The engine's random-boundary strategy records seismograms, misfit and
+residual with the absorbing (CPML) forward, runs a second forward without
 CPML in a seeded random-velocity frame (Clapp, "Reverse time migration with
-random boundaries", SEG 2009) and rebuilds that forward wavefield backwards
-in time for the gradient.  In exact arithmetic this is the reference's
-gradient computed from the stored wavefield of that same forward, which the
+random boundaries", SEG 2009; Shen & Clapp, Geophysics 2015) and rebuilds
+that second wavefield backwards in time for the gradient.  In exact
+arithmetic this is the reference's gradient computed from the residual of
+the CPML forward and the stored wavefield of the frame forward, which the
 oracle gives directly: orc_forward with an identity CPML (a = b = 0, K = 1)
-on the frame materials, then orc_adjoint with the real CPML and medium.
+on the frame materials for the storage, then orc_adjoint with the real CPML
+and medium.
 
 The frame: in the padding, velocities are scaled by f = 1 - alpha (d / ppad) u
 with d the depth into the padding and u = (hash(cell) >> 8) / 2^24, the same
@@ -64,6 +67,6 @@ def gradient(p, obs, shot=0):
     fw = O.forward(q, shot, True, p.lam * f2, p.mu * f2, p.rho,
                    averaged=(mzx * f2[:-1, :-1], rzp, rxp))
     rows = O.shot_rows(p, shot)
-    J, res, _ = O.residual(fw["rec"], obs, p.dt, rows)
+    J, res, _ = O.residual(O.forward(p, shot)["rec"], obs, p.dt, rows)
     ad = O.adjoint(p, shot, res, fw["store"])
     return J, (ad["grad_lam"], ad["grad_mu"], ad["grad_rho"])

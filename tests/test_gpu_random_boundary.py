@@ -1,8 +1,9 @@
 """Random-boundary reconstruction (FWI_STORE_RANDOM) against the FP64 oracle.
 
-The engine rebuilds the random-boundary forward wavefield backwards in time;
-the oracle computes the reference gradient from the stored wavefield of the
-same forward (oracle/random_boundary.py).  The difference is the FP32
+The engine takes the residual from the absorbing forward and rebuilds the
+random-frame forward wavefield backwards in time; the oracle computes the
+reference gradient from the same residual and the stored wavefield of the
+frame forward (oracle/random_boundary.py).  The difference is the FP32
 time-reversal drift plus FP32 arithmetic.
 """
 import numpy as np
@@ -41,7 +42,7 @@ def test_random_boundary_matches_oracle(order, fwi):
     assert mis[0] == pytest.approx(J, rel=1e-4)
     for i in range(3):
         assert rel_l2(g[i][0], g_o[i]) <= 1e-3, i
-    assert st["recompute_steps"] == p.nt
+    assert st["recompute_steps"] == 2 * p.nt
 
 
 def test_random_boundary_batched_gradient_and_cost():
@@ -61,12 +62,10 @@ def test_random_boundary_batched_gradient_and_cost():
     for i in range(3):
         assert rel_l2(g[i], ref[i]) <= 1e-3, i
     assert st["device_bytes"] > 0
-    # interior agreement with the absorbing-boundary gradient (not equal: the
-    # random frame scatters instead of absorbing)
-    z = slice(p.ppad, p.nzt - p.ppad)
-    x = slice(p.ppad, p.nxt - p.ppad)
-    c = np.corrcoef(g[0][z, x].ravel(), gb[0][z, x].ravel())[0, 1]
-    assert c > 0.5
+    # close to the absorbing-boundary gradient: same residual, the source
+    # wavefield differs by what the random frame scatters back
+    for i in range(3):
+        assert rel_l2(g[i], gb[i]) <= 0.5, i
 
 
 def test_random_boundary_refusals():
