@@ -73,6 +73,11 @@ class FwiIter(C.Structure):
 
 TRIAL_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_double, dp)
 
+
+class Model(C.Structure):
+    _fields_ = [("grid", Desc), ("lam", dp), ("mu", dp), ("rho", dp), ("nsrc", C.c_int), ("src_x", ip),
+                ("src_z", ip), ("src_signal", dp), ("nrec", C.c_int), ("rec_x", ip), ("rec_z", ip)]
+
 _lib = None
 
 # (name, restype, argtypes); every int-returning function is a status call.
@@ -109,6 +114,13 @@ _SIGS = {
     "fwi_psv_set_snapshots": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "fwi_psv_snapshot": (C.c_int, [C.c_void_p, C.c_int, C.c_int, dp]),
     "fwi_psv_get_layout": (C.c_int, [C.c_void_p, C.POINTER(Layout)]),
+    "fwi_psv_multi_create": (C.c_int, [C.c_int, C.POINTER(Model), C.c_int, C.POINTER(C.c_void_p)]),
+    "fwi_psv_multi_destroy": (C.c_int, [C.c_void_p]),
+    "fwi_psv_multi_set_exec": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int]),
+    "fwi_psv_multi_gradient": (C.c_int, [C.c_void_p, C.POINTER(dp), dp, C.POINTER(dp), C.POINTER(dp),
+                                         C.POINTER(dp)]),
+    "fwi_psv_multi_tuning": (C.c_int, [C.c_void_p, C.c_int, ip, dp]),
+    "fwi_psv_multi_get_stats": (C.c_int, [C.c_void_p, C.POINTER(Stats)]),
     "fwi_psv_set_model_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "fwi_psv_set_precondition": (C.c_int, [C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_double]),
     "fwi_psv_misfit": (C.c_int, [C.c_void_p, C.c_int, ip, dp, dp, C.c_int]),

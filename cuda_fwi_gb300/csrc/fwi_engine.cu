@@ -1817,6 +1817,8 @@ struct Engine {
 
 }  // namespace fwi
 
+#include "fwi_multi.cuh"
+
 // ===========================================================================
 // C ABI
 // ===========================================================================
@@ -1968,6 +1970,76 @@ int fwi_psv_set_model_lmr(fwi_psv_engine* h, const double* lam, const double* mu
     std::vector<double> mz(na), rz(na), rx(na);
     fwi::average_parameters(e.nzt, e.nxt, mu, rho, mz.data(), rz.data(), rx.data());
     return e.set_model(lam, mu, mz.data(), rz.data(), rx.data());
+}
+
+struct fwi_psv_multi {
+    fwi::MultiEngine m;
+};
+
+int fwi_psv_multi_create(int nmodels, const fwi_psv_model* models, int device, fwi_psv_multi** out) {
+    if (!out) return fail(FWI_ERR_INVALID, "null output handle");
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return fail(FWI_ERR_NODEVICE, "no CUDA device");
+    }
+    if (device < 0 || device >= ndev) return fail(FWI_ERR_INVALID, "bad device index");
+    auto* h = new (std::nothrow) fwi_psv_multi();
+    if (!h) return fail(FWI_ERR_NOMEM, "host allocation failed");
+    const int st = h->m.init(nmodels, models, device);
+    if (st != FWI_OK) {
+        delete h;
+        return st;
+    }
+    *out = h;
+    return FWI_OK;
+}
+
+int fwi_psv_multi_destroy(fwi_psv_multi* h) {
+    if (!h) return FWI_OK;
+    cudaSetDevice(h->m.device);
+    delete h;
+    return FWI_OK;
+}
+
+int fwi_psv_multi_set_exec(fwi_psv_multi* h, int use_graphs, int snapshots, int autotune) {
+    if (!h) return fail(FWI_ERR_INVALID, "null handle");
+    if (snapshots < 0) return fail(FWI_ERR_INVALID, "snapshots must be >= 0");
+    h->m.use_graphs = use_graphs ? 1 : 0;
+    h->m.slots_req = snapshots;
+    h->m.plan.clear();
+    h->m.tune_on = autotune ? 1 : 0;
+    h->m.drop_graphs();
+    return FWI_OK;
+}
+
+int fwi_psv_multi_gradient(fwi_psv_multi* h, const double* const* obs, double* misfit, double* const* gl,
+                           double* const* gm, double* const* gr) {
+    if (!h) return fail(FWI_ERR_INVALID, "null handle");
+    return h->m.gradient(obs, misfit, gl, gm, gr);
+}
+
+int fwi_psv_multi_tuning(fwi_psv_multi* h, int group, int info[7], double ms[2]) {
+    if (!h || !info || !ms) return fail(FWI_ERR_INVALID, "null argument");
+    if (group < 0 || group >= (int)h->m.groups.size()) return fail(FWI_ERR_INVALID, "no such order group");
+    const auto& g = *h->m.groups[group];
+    info[0] = g.fp;
+    info[1] = (int)g.members.size();
+    info[2] = g.kf.map;
+    info[3] = g.tune.ftz;
+    info[4] = g.ka.map;
+    info[5] = g.tune.atz;
+    info[6] = g.tune.cached ? 1 : 0;
+    ms[0] = g.tune.fms;
+    ms[1] = g.tune.ams;
+    return FWI_OK;
+}
+
+int fwi_psv_multi_get_stats(fwi_psv_multi* h, fwi_psv_stats* out) {
+    if (!h || !out) return fail(FWI_ERR_INVALID, "null argument");
+    *out = h->m.stats;
+    return FWI_OK;
 }
 
 int fwi_psv_set_snapshots(fwi_psv_engine* h, int interval, int which) {

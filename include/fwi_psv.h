@@ -344,6 +344,44 @@ typedef int (*fwi_psv_trial_fn)(void* ctx, double step, double* misfit);
 int fwi_psv_step_search(double est, double L2_0, fwi_psv_trial_fn trial, void* ctx, double* opt,
                         int* trials, int* status);
 
+/* ---- independent models in one launch ------------------------------------
+ * Many models of uneven grid size, fdorder and nt (one shot each) advanced
+ * together: every pass of a time step is one launch per fdorder over the
+ * tiles of all models still running (models sorted by nt, tiles model-major),
+ * one binomial reversal plan over the longest nt serves every model, and the
+ * whole gradient is replayed as CUDA graphs.  Each model is the reference's
+ * per-shot call (forward_kernel_PSV_GPU + adjoint_kernel_PSV_GPU with the
+ * reference gradient, fwi intervals 1, window = the padded grid from the free
+ * surface down).  The thread mapping and tile height of each fdorder group are
+ * chosen by timing the candidates on the group's own tiles (autotune != 0),
+ * cached in a JSON file ($FWI_PSV_TUNE_CACHE, default
+ * ~/.cache/cuda_fwi_gb300/autotune.json) keyed by GPU and group shape. */
+typedef struct fwi_psv_model {
+    fwi_psv_desc grid;                 /* as for fwi_psv_create */
+    const double *lam, *mu, *rho;      /* [nzt][nxt] */
+    int nsrc;                          /* vz sources (padded indices) */
+    const int *src_x, *src_z;
+    const double* src_signal;          /* [nsrc][nt] */
+    int nrec;                          /* vz receivers (padded indices) */
+    const int *rec_x, *rec_z;
+} fwi_psv_model;
+typedef struct fwi_psv_multi fwi_psv_multi;
+int fwi_psv_multi_create(int nmodels, const fwi_psv_model* models, int device, fwi_psv_multi** out);
+int fwi_psv_multi_destroy(fwi_psv_multi* m);
+/* use_graphs (default 1); snapshots = checkpoint slots of the common plan
+ * (default 32; 0 = as many as 80% of free memory holds); autotune (default 1). */
+int fwi_psv_multi_set_exec(fwi_psv_multi* m, int use_graphs, int snapshots, int autotune);
+/* obs[k] [nrec_k][nt_k]; misfit[k]; grad_*[k] [nzt_k][nxt_k] (any may be NULL). */
+int fwi_psv_multi_gradient(fwi_psv_multi* m, const double* const* obs, double* misfit,
+                           double* const* grad_lam, double* const* grad_mu, double* const* grad_rho);
+/* Choice for order group g (after the first gradient when autotuning):
+ * info = {half order, models, forward mapping, forward tile rows, adjoint mapping,
+ * adjoint tile rows, read from the cache (1) or timed now (0)}; ms = {forward pair,
+ * adjoint stress} per launch over the whole group, as timed when the choice was made
+ * (the cache keeps them).  Mappings: 0 z-march (tile rows), 1 scalar cells, 2 vectorised cells. */
+int fwi_psv_multi_tuning(fwi_psv_multi* m, int group, int info[7], double ms[2]);
+int fwi_psv_multi_get_stats(fwi_psv_multi* m, fwi_psv_stats* out);
+
 /* ---- allocation-free misfit ---------------------------------------------- */
 
 /* No counterpart in the reference (whose misfit, calculate_l2_adjoint_sources,
