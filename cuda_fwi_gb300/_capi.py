@@ -117,6 +117,7 @@ _SIGS = {
     "fwi_psv_multi_create": (C.c_int, [C.c_int, C.POINTER(Model), C.c_int, C.POINTER(C.c_void_p)]),
     "fwi_psv_multi_destroy": (C.c_int, [C.c_void_p]),
     "fwi_psv_multi_set_exec": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int]),
+    "fwi_psv_multi_forward": (C.c_int, [C.c_void_p, C.POINTER(dp)]),
     "fwi_psv_multi_gradient": (C.c_int, [C.c_void_p, C.POINTER(dp), dp, C.POINTER(dp), C.POINTER(dp),
                                          C.POINTER(dp)]),
     "fwi_psv_multi_tuning": (C.c_int, [C.c_void_p, C.c_int, ip, dp]),

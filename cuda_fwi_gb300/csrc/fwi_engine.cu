@@ -2014,6 +2014,11 @@ int fwi_psv_multi_set_exec(fwi_psv_multi* h, int use_graphs, int snapshots, int 
     return FWI_OK;
 }
 
+int fwi_psv_multi_forward(fwi_psv_multi* h, double* const* rec_out) {
+    if (!h) return fail(FWI_ERR_INVALID, "null handle");
+    return h->m.forward(rec_out);
+}
+
 int fwi_psv_multi_gradient(fwi_psv_multi* h, const double* const* obs, double* misfit, double* const* gl,
                            double* const* gm, double* const* gr) {
     if (!h) return fail(FWI_ERR_INVALID, "null handle");

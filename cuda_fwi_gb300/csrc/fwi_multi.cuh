@@ -606,6 +606,34 @@ struct MultiEngine {
         return FWI_OK;
     }
 
+    // ---- forward modelling only -------------------------------------------------
+    int forward(double* const* rec_out) {
+        FWI_TRY(bind());
+        launches_now = 0;
+        FWI_TRY(run_phase("fwdonly", [&]() -> int {
+            CUDA_TRY(cudaMemsetAsync(d_fwd.p, 0, total_state * 4, stream));
+            CUDA_TRY(cudaMemsetAsync(d_ws.p, 0, total_field * 4, stream));
+            CUDA_TRY(cudaMemsetAsync(d_rec.p, 0, total_rec * 4, stream));
+            forward_steps(0, nt_max, true);
+            return FWI_OK;
+        }));
+        std::vector<float> h(total_rec);
+        CUDA_TRY(cudaMemcpyAsync(h.data(), d_rec.p, total_rec * 4, cudaMemcpyDeviceToHost, stream));
+        CUDA_TRY(cudaStreamSynchronize(stream));
+        int flag = 0;
+        CUDA_TRY(cudaMemcpy(&flag, d_err.p, 4, cudaMemcpyDeviceToHost));
+        if (flag) return fail(FWI_ERR_CUDA, "a kernel raised its error flag; results discarded");
+        for (int b = 0; b < n; b++)
+            if (rec_out && rec_out[b])
+                for (size_t i = 0; i < (size_t)items[b].nrec * items[b].nt; i++)
+                    rec_out[b][i] = h[items[b].off_rec + i];
+        stats = fwi_psv_stats{};
+        stats.launches = launches_now;
+        stats.forward_steps = nt_max;
+        stats.batch = n;
+        return FWI_OK;
+    }
+
     // ---- gradient ---------------------------------------------------------------
     int gradient(const double* const* obs, double* misfit, double* const* gl, double* const* gm,
                  double* const* gr) {

@@ -68,6 +68,14 @@ class MultiEngine:
         """Rows of problem k's [nrec][nt] observed-data array that the engine uses (shot 0, vz)."""
         return np.nonzero(self._keep[k][7])[0]
 
+    def forward(self):
+        """vz traces of every model: list of [nrec_k][nt_k] arrays (the receivers of shot 0)."""
+        n = len(self.ps)
+        recs = [np.zeros((len(self.receiver_rows(k)), p.nt)) for k, p in enumerate(self.ps)]
+        arr = (_capi.dp * n)(*[pd(r) for r in recs])
+        check(_capi.lib().fwi_psv_multi_forward(self.h, arr), "fwi_psv_multi_forward")
+        return recs
+
     def gradient(self, obs, want=True):
         """obs: list of [nrec][nt] arrays (the problem's receiver order; rows of
         shot 0 are used).  Returns ([(g_lam, g_mu, g_rho)] per model, misfits)."""

@@ -371,6 +371,9 @@ int fwi_psv_multi_destroy(fwi_psv_multi* m);
 /* use_graphs (default 1); snapshots = checkpoint slots of the common plan
  * (default 32; 0 = as many as 80% of free memory holds); autotune (default 1). */
 int fwi_psv_multi_set_exec(fwi_psv_multi* m, int use_graphs, int snapshots, int autotune);
+/* Forward modelling of every model (forward_simulate, fd_wave_model.cu:133-230):
+ * rec_out[k] [nrec_k][nt_k] receives model k's vz traces (NULL entries skipped). */
+int fwi_psv_multi_forward(fwi_psv_multi* m, double* const* rec_out);
 /* obs[k] [nrec_k][nt_k]; misfit[k]; grad_*[k] [nzt_k][nxt_k] (any may be NULL). */
 int fwi_psv_multi_gradient(fwi_psv_multi* m, const double* const* obs, double* misfit,
                            double* const* grad_lam, double* const* grad_mu, double* const* grad_rho);

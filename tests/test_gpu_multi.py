@@ -58,6 +58,11 @@ def test_uneven_models_match_oracle(tune_cache):
         assert mis[k] == pytest.approx(J, rel=1e-4), k
         for i in range(3):
             assert rel_l2(grads[k][i], _oracle_grid(p, g_o[i])) <= 1e-4, (k, i)
+    with MultiEngine(ps, snapshots=6) as m:
+        recs = m.forward()
+    for k, p in enumerate(ps):
+        want = O.forward(p, 0)["rec"][m.receiver_rows(k)]
+        assert rel_l2(recs[k], want) <= 1e-5, k
     assert sorted(t["half_order"] for t in tun) == [2, 4]
     assert sum(t["models"] for t in tun) == len(ps)
     assert st["forward_steps"] == max(s["nt"] for s in SPECS)
