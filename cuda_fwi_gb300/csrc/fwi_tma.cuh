@@ -667,7 +667,12 @@ __device__ __forceinline__ void adjoint_compute(const ItemDesc& D, const float* 
     // gradient window column of this thread
     int xf = -1;
     const int wz1 = D.wz1, wz2 = D.wz2, fdz = D.fwi_dz, nfx = D.nfx;
-    if (grad_step && ix >= D.wx1 && ix < D.wx2 && (ix - D.wx1) % D.fwi_dx == 0) xf = (ix - D.wx1) / D.fwi_dx;
+    if (grad_step && ix >= D.wx1 && ix < D.wx2) {
+        // unit intervals (the common case) need no integer division
+        const int dxw = ix - D.wx1;
+        if (D.fwi_dx == 1) xf = dxw;
+        else if (dxw % D.fwi_dx == 0) xf = dxw / D.fwi_dx;
+    }
     float* __restrict__ glam = D.glam;
     float* __restrict__ gmu = D.gmu;
     float* __restrict__ grho = D.grho;
@@ -693,8 +698,8 @@ __device__ __forceinline__ void adjoint_compute(const ItemDesc& D, const float* 
             mz2[rr] = mvx_z[(size_t)pz * P + ix];
         }
         gi[rr] = -1;
-        if (xf >= 0 && iz < nzt - FP && iz >= wz1 && iz < wz2 && (iz - wz1) % fdz == 0) {
-            gi[rr] = ((iz - wz1) / fdz) * nfx + xf;
+        if (xf >= 0 && iz < nzt - FP && iz >= wz1 && iz < wz2 && (fdz == 1 || (iz - wz1) % fdz == 0)) {
+            gi[rr] = (fdz == 1 ? iz - wz1 : (iz - wz1) / fdz) * nfx + xf;
             g0[rr] = glam[gi[rr]];
             g1[rr] = gmu[gi[rr]];
             g2[rr] = grho[gi[rr]];
@@ -745,13 +750,17 @@ __device__ __forceinline__ void adjoint_compute(const ItemDesc& D, const float* 
         gux[c] = ux;
         guz[c] = uz;
         if (gi[rr] >= 0) {
-            const float fvx = cen[8 * G::CEN + ci] / dt, fvz = cen[9 * G::CEN + ci] / dt;
+            // the stored velocities are v/dt; reciprocals computed once per cell
+            // (two divisions instead of five; rounding within the gradient tolerance)
+            const float fvx = cen[8 * G::CEN + ci] * inv_dt, fvz = cen[9 * G::CEN + ci] * inv_dt;
             const float fsxx = cen[10 * G::CEN + ci], fszx = cen[11 * G::CEN + ci], fszz = cen[12 * G::CEN + ci];
             const float lpm = (L + 0.5f * M2) * inv_dt;
             const float mu = 0.5f * M2 * inv_dt;
-            const float s1 = (fsxx + fszz) * (sxx + szz) * 0.25f / (lpm * lpm);
-            const float s2 = (fsxx - fszz) * (sxx - szz) / (mu * mu);
-            const float s3 = (fszx * szx) / (mu * mu);
+            const float ilpm2 = 0.25f / (lpm * lpm);
+            const float imu2 = 1.f / (mu * mu);
+            const float s1 = (fsxx + fszz) * (sxx + szz) * ilpm2;
+            const float s2 = (fsxx - fszz) * (sxx - szz) * imu2;
+            const float s3 = (fszx * szx) * imu2;
             const float s4 = ux * fvx + uz * fvz;
             glam[gi[rr]] = g0[rr] + gs * s1;
             gmu[gi[rr]] = g1[rr] + gs * (s3 + s1 + s2);
