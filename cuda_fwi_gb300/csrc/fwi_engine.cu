@@ -1108,9 +1108,22 @@ struct Engine {
         tgrid.nb = B;
         tgrid.ntz = ntz;
         tgrid.ntiles = B * ntz * ntx;
+        // plain-stencil cells of both forward passes (the CPML rule also covers
+        // the random-frame sweeps, which have no strips)
+        tgrid.cxl = fpad;
+        tgrid.cxh = nxt - fpad - 1;
+        tgrid.czl = fpad;
+        tgrid.czh = nzt - fpad - 1;
+        if (npml > 0) {
+            tgrid.cxl = std::max(tgrid.cxl, ppad + 1);
+            tgrid.cxh = std::min(tgrid.cxh, nxt - ppad - 2);
+            tgrid.czh = std::min(tgrid.czh, nzt - ppad - 2);
+            if (!fsurf) tgrid.czl = std::max(tgrid.czl, ppad + 1);
+        }
+        if (fsurf) tgrid.czl = std::max(tgrid.czl, 2 * fpad + 1);
         grid_tma = std::max(1, std::min(tgrid.ntiles, num_sms));
         const int ntz_a = (nzt - 2 * fpad + kAdjTZ - 1) / kAdjTZ;
-        tgrid_a.nb = B;
+        tgrid_a = tgrid;
         tgrid_a.ntz = ntz_a;
         tgrid_a.ntiles = B * ntz_a * ntx;
         grid_tma_a = std::max(1, std::min(tgrid_a.ntiles, num_sms));

@@ -33,8 +33,7 @@ namespace fwi {
 
 constexpr int kTmaTX = 128;      // tile columns
 constexpr int kTmaTZ = 16;       // tile rows
-constexpr int kTmaThreads = 512; // 4 threads per column (4 rows each in a 16-row tile)
-constexpr int kThreadRowsF = kTmaTZ / (kTmaThreads / kTmaTX);  // rows per thread, forward passes
+constexpr int kTmaThreads = 512; // forward: a column pair and two rows each; adjoint: a column and two rows
 // stages in flight per CTA: three while they fit the 227 KB of shared memory
 // (half orders up to 4), two above
 template <int FP>
@@ -76,8 +75,12 @@ struct VelMaps {
 
 // Tile t of a launch: slot b = t % nb (shots minor, so consecutive CTAs share
 // the material tile in L2), then z-tile, then x-tile.
+// [cxl, cxh] x [czl, czh] (inclusive) are the cells that both forward passes
+// update with the plain stencil: no border column, no CPML strip (taken one
+// cell wider than either pass uses it), no free-surface row or mirror row.
 struct TmaGrid {
     int nb, ntz, ntiles, pad;
+    int cxl, cxh, czl, czh;
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -148,14 +151,159 @@ __device__ __forceinline__ void tile_coords(const TmaGrid& g, int t, int* b, int
 }
 
 // ---------------------------------------------------------------------------
+// two-cell arithmetic of the forward passes
+// ---------------------------------------------------------------------------
+// In the stress and velocity passes a thread owns two neighbouring columns of
+// two rows.  Staged values are read as 8-byte pairs and every stencil operation
+// is one FP32x2 instruction for both columns (each lane rounded like the
+// scalar operation), which halves the load and arithmetic instructions per
+// cell of the one-column mapping.
+constexpr int kPairRows = 2;  // rows per thread (64 column pairs x 8 row groups = 128 x 16)
+static_assert((kTmaTX / 2) * (kTmaTZ / kPairRows) == kTmaThreads, "one thread per column pair and row pair");
+static_assert(kTmaTX == 128 && kPairRows == 2, "a warp covers 64 columns of one row pair");
+
+__device__ __forceinline__ float2 bc2(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) {
+    float2 d;
+    asm("{\n\t.reg .b64 ra, rb, rd;\n\tmov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t"
+        "sub.rn.f32x2 rd, ra, rb;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+        : "=f"(d.x), "=f"(d.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return d;
+}
+__device__ __forceinline__ float2 ld2(const float* p) { return *reinterpret_cast<const float2*>(p); }
+__device__ __forceinline__ float lane(float2 v, int l) { return l ? v.y : v.x; }
+// store a pair, or only its lanes inside the updated columns
+__device__ __forceinline__ void st2(float* p, float2 v, bool on0, bool on1) {
+    if (on0 && on1) {
+        *reinterpret_cast<float2*>(p) = v;
+    } else {
+        if (on0) p[0] = v.x;
+        if (on1) p[1] = v.y;
+    }
+}
+
+// One staged row around a column pair (pointer p at the pair's first column,
+// 8-byte aligned): q[j] is the pair at column offset 2j - E, E = FP rounded up
+// to even, so at(i) covers offsets -E .. FP+1.  The pair at offset 0 is the
+// caller's (it is the centre of a z-window already in registers).
+template <int FP>
+struct RowPairs {
+    static constexpr int E = 2 * ((FP + 1) / 2);
+    static constexpr int NQ = (E + FP + 1) / 2 + 1;
+    float2 q[NQ];
+    __device__ __forceinline__ void load(const float* p, float2 centre) {
+#pragma unroll
+        for (int j = 0; j < NQ; j++) q[j] = (2 * j == E) ? centre : ld2(p + 2 * j - E);
+    }
+    __device__ __forceinline__ float at(int i) const {
+        const int u = i + E;
+        return (u & 1) ? q[u >> 1].y : q[u >> 1].x;
+    }
+    // (f[c+i] - f[c+j], f[c+i+1] - f[c+j+1]); an odd offset is a pair that
+    // straddles two loaded pairs, and then the lanes are subtracted one by one
+    // straight into a fresh register pair (no copies to assemble the operand)
+    __device__ __forceinline__ float2 diff(int i, int j) const {
+        if ((((i + E) | (j + E)) & 1) == 0) return sub2(q[(i + E) >> 1], q[(j + E) >> 1]);
+        return make_float2(__fsub_rn(at(i), at(j)), __fsub_rn(at(i + 1), at(j + 1)));
+    }
+    // sum_k h_k (f[c+k-1] - f[c-k]) for c and c+1
+    __device__ __forceinline__ float2 dminus(const float2* h) const {
+        float2 d = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int k = 1; k <= FP; k++) d = fma2(h[k - 1], diff(k - 1, -k), d);
+        return d;
+    }
+    // sum_k h_k (f[c+k] - f[c-k+1]) for c and c+1
+    __device__ __forceinline__ float2 dplus(const float2* h) const {
+        float2 d = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int k = 1; k <= FP; k++) d = fma2(h[k - 1], diff(k, 1 - k), d);
+        return d;
+    }
+};
+
+// The warp's 64 columns x kPairRows rows lie inside the grid's plain-stencil
+// cells and no storage sample is taken: it runs the branch-free row loop.
+// The decision is the same for every thread of the warp.
+__device__ __forceinline__ bool interior_warp(const TmaGrid& g, int x0, int z0, unsigned flags) {
+    const int w = threadIdx.x >> 5;
+    const int wx0 = x0 + (w & 1) * 64, wz0 = z0 + (w >> 1) * 2;
+    return !(flags & FL_STORE) && wx0 >= g.cxl && wx0 + 63 <= g.cxh && wz0 >= g.czl && wz0 + 1 <= g.czh;
+}
+
+// Columns of a pair that the pass updates, and their x-strip indices.
+struct PairCols {
+    bool on0, on1;
+    int px[2];
+};
+template <int FP>
+__device__ __forceinline__ PairCols pair_cols(const ItemDesc& D, int ix, bool stress) {
+    PairCols pc;
+    pc.on0 = ix >= FP && ix < D.nxt - FP;
+    pc.on1 = ix + 1 >= FP && ix + 1 < D.nxt - FP;
+#pragma unroll
+    for (int l = 0; l < 2; l++) {
+        const int i = ix + l;
+        int px = -1;
+        if (D.npml > 0 && (l ? pc.on1 : pc.on0)) {
+            // the stress pass's left strip includes column ppad, the velocity pass's does not
+            if (stress ? i <= D.ppad : i < D.ppad) px = i - FP;
+            else if (i >= D.nxt - D.ppad - 1) px = i - D.pnx;
+            if (px == D.npml) px = -1;
+        }
+        pc.px[l] = px;
+    }
+    return pc;
+}
+
+// CPML of an x-derivative pair (d1 with the integer-grid coefficients, d2 with
+// the half-grid ones): memories m1/m2 of each lane in an x-strip are advanced
+// and stored, and the lane's derivatives corrected.  The coefficients are
+// re-read per row (L1 hits) rather than held in registers by every thread.
+__device__ __forceinline__ void cpml_x_pair(const PairCols& pc, const float* __restrict__ cpml, int iz, int tp,
+                                            const float (&o1)[2], const float (&o2)[2], float* __restrict__ a1,
+                                            float* __restrict__ a2, float2& d1, float2& d2) {
+#pragma unroll
+    for (int l = 0; l < 2; l++) {
+        if (pc.px[l] >= 0) {
+            const Cpml c = load_cpml(cpml, tp, pc.px[l]);
+            float& e1 = l ? d1.y : d1.x;
+            float& e2 = l ? d2.y : d2.x;
+            const size_t m = (size_t)iz * tp + pc.px[l];
+            const float m1 = c.b * o1[l] + c.a * e1;
+            const float m2 = c.bh * o2[l] + c.ah * e2;
+            a1[m] = m1;
+            a2[m] = m2;
+            e1 = e1 * c.iK + m1;
+            e2 = e2 * c.iKh + m2;
+        }
+    }
+}
+
+// z-strip index of row iz (-1 outside the strips); the stress pass's top strip
+// includes row ppad, the velocity pass's does not.
+template <int FP>
+__device__ __forceinline__ int strip_z(const ItemDesc& D, int iz, bool stress) {
+    int pz = -1;
+    if (D.npml > 0 && iz < D.nzt - FP) {
+        if (!D.fsurf && (stress ? iz <= D.ppad : iz < D.ppad)) pz = iz - FP;
+        else if (iz >= D.nzt - D.ppad - 1) pz = iz - D.pnz;
+        if (pz == D.npml) pz = -1;
+    }
+    return pz;
+}
+
+// ---------------------------------------------------------------------------
 // stress pass
 // ---------------------------------------------------------------------------
 template <int FP>
-__device__ __forceinline__ void stress_issue(const StressMaps& m, const ItemDesc* items, const TmaGrid& g, int t,
+__device__ __forceinline__ void stress_issue(const StressMaps& m, const ItemDesc* items, int b, int x0, int z0,
                                              float* st, uint64_t* bar) {
     using G = TmaGeom<FP>;
-    int b, x0, z0;
-    tile_coords(g, t, &b, &x0, &z0, FP);
     constexpr unsigned bytes = 4u * (2 * G::WX * G::WZ + 6 * G::CEN) + (unsigned)sizeof(ItemDesc);
     mbar_expect_tx(bar, bytes);
     bulk_load(st + G::S_DESC, items + b, (unsigned)sizeof(ItemDesc), bar);
@@ -170,38 +318,33 @@ __device__ __forceinline__ void stress_issue(const StressMaps& m, const ItemDesc
     tma_load_3d(c + 5 * G::CEN, &m.szz, x0, z0, b, bar);
 }
 
-template <int FP>
-__device__ __forceinline__ void stress_compute(const ItemDesc& D, const float* st, int x0, int z0, int it,
-                                               unsigned flags) {
+template <int FP, bool INTERIOR>
+__device__ __forceinline__ void stress_rows(const ItemDesc& D, const float* st, int x0, int z0, int it,
+                                            unsigned flags, const float2 (&hx)[FP], const float2 (&hz)[FP]) {
     using G = TmaGeom<FP>;
-    constexpr int R = kThreadRowsF;  // rows of this thread
-    const int tx = threadIdx.x & (kTmaTX - 1);
-    const int r0 = (threadIdx.x / kTmaTX) * R;
-    const int ix = x0 + tx;
-    const int nxt = D.nxt, nzt = D.nzt, P = D.pitch;
-    if (ix < FP || ix >= nxt - FP) return;
-    float hx[FP], hz[FP];
-#pragma unroll
-    for (int k = 0; k < FP; k++) {
-        hx[k] = D.hx[k];
-        hz[k] = D.hz[k];
+    constexpr int R = kPairRows;
+    constexpr int W = R + 2 * FP - 1;
+    const int cp = (threadIdx.x & (kTmaTX / 2 - 1)) * 2;  // tile column of the pair
+    const int r0 = (threadIdx.x / (kTmaTX / 2)) * R;
+    const int ix = x0 + cp;
+    PairCols pc = {true, true, {-1, -1}};
+    if constexpr (!INTERIOR) {
+        pc = pair_cols<FP>(D, ix, true);
+        if (!pc.on0 && !pc.on1) return;
     }
+    const int nzt = D.nzt, P = D.pitch, tp = D.tp;
     const float* svx = st;
     const float* svz = st + G::HXZ;
     const float* cen = st + 2 * G::HXZ;
-    const int col = tx + G::HX;
-    // z-windows of this thread's rows: wvx[j] = vx of row r0 + j - FP + 1,
-    // wvz[j] = vz of row r0 + j - FP (each staged value read once)
-    float wvx[R + 2 * FP - 1], wvz[R + 2 * FP - 1];
+    const int col = cp + G::HX;
+    // z-windows: wvx[j] = vx pair of row r0 + j - FP + 1, wvz[j] = vz pair of row r0 + j - FP
+    float2 wvx[W], wvz[W];
 #pragma unroll
-    for (int j = 0; j < R + 2 * FP - 1; j++) {
-        wvx[j] = svx[(r0 + j + 1) * G::WX + col];
-        wvz[j] = svz[(r0 + j) * G::WX + col];
+    for (int j = 0; j < W; j++) {
+        wvx[j] = ld2(svx + (r0 + j + 1) * G::WX + col);
+        wvz[j] = ld2(svz + (r0 + j) * G::WX + col);
     }
-    const float dt = D.dt;
-    const int ppad = D.ppad, npml = D.npml, tp = D.tp, pnz = D.pnz;
     const bool fsurf = D.fsurf != 0;
-    const float* __restrict__ cpml = D.cpml;
     float* __restrict__ gsxx = D.sxx;
     float* __restrict__ gszx = D.szx;
     float* __restrict__ gszz = D.szz;
@@ -209,122 +352,137 @@ __device__ __forceinline__ void stress_compute(const ItemDesc& D, const float* s
     float* __restrict__ mvz_x = D.mvz_x;
     float* __restrict__ mvx_z = D.mvx_z;
     float* __restrict__ mvz_z = D.mvz_z;
-    int px = -1;
-    if (npml > 0) {
-        if (ix <= ppad) px = ix - FP;
-        else if (ix >= nxt - ppad - 1) px = ix - D.pnx;
-        if (px == npml) px = -1;
-    }
-    Cpml cx = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    if (px >= 0) cx = load_cpml(cpml, tp, px);
-    // CPML memories of all rows of this thread, loaded before any row is
-    // computed (one memory latency per tile instead of one per row)
-    float mx1[R], mx2[R], mz1[R], mz2[R];
+    // CPML memories of both rows, loaded before any row is computed
+    float mx1[R][2], mx2[R][2];
+    float2 mz1[R], mz2[R];
     int pzr[R];
+    int xf[2] = {-1, -1};
+    if constexpr (!INTERIOR) {
 #pragma unroll
-    for (int rr = 0; rr < R; rr++) {
-        const int iz = z0 + r0 + rr;
-        mx1[rr] = mx2[rr] = mz1[rr] = mz2[rr] = 0.f;
-        int pz = -1;
-        if (npml > 0 && iz < nzt - FP) {
-            if (!fsurf && iz <= ppad) pz = iz - FP;
-            else if (iz >= nzt - ppad - 1) pz = iz - pnz;
-            if (pz == npml) pz = -1;
+        for (int rr = 0; rr < R; rr++) {
+            const int iz = z0 + r0 + rr;
+            mz1[rr] = mz2[rr] = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int l = 0; l < 2; l++) {
+                mx1[rr][l] = mx2[rr][l] = 0.f;
+                if (pc.px[l] >= 0 && iz < nzt - FP) {
+                    mx1[rr][l] = mvx_x[(size_t)iz * tp + pc.px[l]];
+                    mx2[rr][l] = mvz_x[(size_t)iz * tp + pc.px[l]];
+                }
+            }
+            pzr[rr] = strip_z<FP>(D, iz, true);
+            if (pzr[rr] >= 0) {
+                mz1[rr] = ld2(mvz_z + (size_t)pzr[rr] * P + ix);
+                mz2[rr] = ld2(mvx_z + (size_t)pzr[rr] * P + ix);
+            }
         }
-        pzr[rr] = pz;
-        if (px >= 0 && iz < nzt - FP) {
-            mx1[rr] = mvx_x[(size_t)iz * tp + px];
-            mx2[rr] = mvz_x[(size_t)iz * tp + px];
-        }
-        if (pz >= 0) {
-            mz1[rr] = mvz_z[(size_t)pz * P + ix];
-            mz2[rr] = mvx_z[(size_t)pz * P + ix];
+        // sampled window columns (forward storage for the gradient)
+        if ((flags & FL_STORE) && D.store) {
+#pragma unroll
+            for (int l = 0; l < 2; l++) {
+                const int i = ix + l;
+                if ((l ? pc.on1 : pc.on0) && i >= D.wx1 && i < D.wx2 && (i - D.wx1) % D.fwi_dx == 0)
+                    xf[l] = (i - D.wx1) / D.fwi_dx;
+            }
         }
     }
-    int xf = -1;
-    if ((flags & FL_STORE) && D.store && ix >= D.wx1 && ix < D.wx2 && (ix - D.wx1) % D.fwi_dx == 0)
-        xf = (ix - D.wx1) / D.fwi_dx;
     // FL_REVERSE undoes the step (s^n = s^{n+1} - S(v^n)); used only without
     // CPML and free surface, where the update is a pure increment
-    const float sg = (flags & FL_REVERSE) ? -1.f : 1.f;
+    const float2 sg = bc2((flags & FL_REVERSE) ? -1.f : 1.f);
+    size_t c = (size_t)(z0 + r0) * P + ix;  // global index of the pair in the current row
 #pragma unroll
-    for (int rr = 0; rr < R; rr++) {
+    for (int rr = 0; rr < R; rr++, c += P) {
         const int r = r0 + rr;
         const int iz = z0 + r;
-        if (iz >= nzt - FP) break;
+        if constexpr (!INTERIOR) {
+            if (iz >= nzt - FP) break;
+        }
         const int row = r + FP;
-        const float* vxr = svx + row * G::WX + col;
-        const float* vzr = svz + row * G::WX + col;
-        float vx_x = 0.f, vz_x = 0.f, vx_z = 0.f, vz_z = 0.f;
+        RowPairs<FP> tvx, tvz;
+        tvx.load(svx + row * G::WX + col, wvx[rr + FP - 1]);
+        tvz.load(svz + row * G::WX + col, wvz[rr + FP]);
+        float2 vx_x = tvx.dminus(hx);
+        float2 vz_x = tvz.dplus(hx);
+        float2 vx_z = make_float2(0.f, 0.f), vz_z = make_float2(0.f, 0.f);
 #pragma unroll
         for (int k = 1; k <= FP; k++) {
-            vx_x += hx[k - 1] * ((k == 1 ? wvx[rr + FP - 1] : vxr[k - 1]) - vxr[-k]);
-            vz_x += hx[k - 1] * (vzr[k] - (k == 1 ? wvz[rr + FP] : vzr[-k + 1]));
-            vx_z += hz[k - 1] * (wvx[rr + k + FP - 1] - wvx[rr - k + FP]);
-            vz_z += hz[k - 1] * (wvz[rr + k - 1 + FP] - wvz[rr - k + FP]);
+            vx_z = fma2(hz[k - 1], sub2(wvx[rr + k + FP - 1], wvx[rr - k + FP]), vx_z);
+            vz_z = fma2(hz[k - 1], sub2(wvz[rr + k - 1 + FP], wvz[rr - k + FP]), vz_z);
         }
-        const size_t c = (size_t)iz * P + ix;
-        if (px >= 0) {
-            const size_t m = (size_t)iz * tp + px;
-            const float m1 = cx.b * mx1[rr] + cx.a * vx_x;
-            const float m2 = cx.bh * mx2[rr] + cx.ah * vz_x;
-            mvx_x[m] = m1;
-            mvz_x[m] = m2;
-            vx_x = vx_x * cx.iK + m1;
-            vz_x = vz_x * cx.iKh + m2;
+        if constexpr (!INTERIOR) {
+            cpml_x_pair(pc, D.cpml, iz, tp, mx1[rr], mx2[rr], mvx_x, mvz_x, vx_x, vz_x);
+            if (pzr[rr] >= 0) {
+                const Cpml cz = load_cpml(D.cpml, tp, pzr[rr]);
+                const size_t m = (size_t)pzr[rr] * P + ix;
+                const float2 m1 = fma2(bc2(cz.b), mz1[rr], mul2(bc2(cz.a), vz_z));
+                const float2 m2 = fma2(bc2(cz.bh), mz2[rr], mul2(bc2(cz.ah), vx_z));
+                st2(mvz_z + m, m1, pc.on0, pc.on1);
+                st2(mvx_z + m, m2, pc.on0, pc.on1);
+                vz_z = fma2(vz_z, bc2(cz.iK), m1);
+                vx_z = fma2(vx_z, bc2(cz.iKh), m2);
+            }
         }
-        if (pzr[rr] >= 0) {
-            const int pz = pzr[rr];
-            const Cpml cz = load_cpml(cpml, tp, pz);
-            const size_t m = (size_t)pz * P + ix;
-            const float m1 = cz.b * mz1[rr] + cz.a * vz_z;
-            const float m2 = cz.bh * mz2[rr] + cz.ah * vx_z;
-            mvz_z[m] = m1;
-            mvx_z[m] = m2;
-            vz_z = vz_z * cz.iK + m1;
-            vx_z = vx_z * cz.iKh + m2;
+        const int ci = r * kTmaTX + cp;
+        const float2 L = ld2(cen + ci), M2 = ld2(cen + G::CEN + ci), MZ = ld2(cen + 2 * G::CEN + ci);
+        float2 sxx = ld2(cen + 3 * G::CEN + ci), szx = ld2(cen + 4 * G::CEN + ci), szz = ld2(cen + 5 * G::CEN + ci);
+        if constexpr (!INTERIOR) {
+            if ((xf[0] >= 0 || xf[1] >= 0) && iz >= D.wz1 && iz < D.wz2 && (iz - D.wz1) % D.fwi_dz == 0) {
+                const size_t fs = (size_t)D.nfz * D.nfx;
+                float* s = D.store + (size_t)(it / D.fwi_dt) * 5 * fs + (size_t)((iz - D.wz1) / D.fwi_dz) * D.nfx;
+#pragma unroll
+                for (int l = 0; l < 2; l++) {
+                    if (xf[l] < 0) continue;
+                    float* q = s + xf[l];
+                    q[F_VX * fs] = lane(wvx[rr + FP - 1], l) / D.dt;
+                    q[F_VZ * fs] = lane(wvz[rr + FP], l) / D.dt;
+                    q[F_SXX * fs] = lane(sxx, l);
+                    q[F_SZX * fs] = lane(szx, l);
+                    q[F_SZZ * fs] = lane(szz, l);
+                }
+            }
         }
-        const int ci = r * kTmaTX + tx;
-        const float L = cen[ci], M2 = cen[G::CEN + ci], MZ = cen[2 * G::CEN + ci];
-        float sxx = cen[3 * G::CEN + ci], szx = cen[4 * G::CEN + ci], szz = cen[5 * G::CEN + ci];
-        if (xf >= 0 && iz >= D.wz1 && iz < D.wz2 && (iz - D.wz1) % D.fwi_dz == 0) {
-            const size_t fs = (size_t)D.nfz * D.nfx;
-            float* s = D.store + (size_t)(it / D.fwi_dt) * 5 * fs + (size_t)((iz - D.wz1) / D.fwi_dz) * D.nfx + xf;
-            s[F_VX * fs] = wvx[rr + FP - 1] / dt;
-            s[F_VZ * fs] = wvz[rr + FP] / dt;
-            s[F_SXX * fs] = sxx;
-            s[F_SZX * fs] = szx;
-            s[F_SZZ * fs] = szz;
-        }
-        szx += sg * (MZ * (vz_x + vx_z));
-        const float tr = L * (vx_x + vz_z);
-        sxx += sg * (tr + M2 * vx_x);
-        szz += sg * (tr + M2 * vz_z);
-        if (fsurf && iz == FP) {
-            szz = 0.f;
-            szx = 0.f;
-            sxx = vx_x * (2.f * M2 * (L + 0.5f * M2)) / (L + M2);
-        }
-        gsxx[c] = sxx;
-        gszx[c] = szx;
-        gszz[c] = szz;
-        if (fsurf && iz > FP && iz <= 2 * FP) {
-            const size_t cm = (size_t)(2 * FP - iz) * P + ix;
-            gszx[cm] = -szx;
-            gszz[cm] = -szz;
+        szx = fma2(sg, mul2(MZ, add2(vz_x, vx_z)), szx);
+        const float2 tr = mul2(L, add2(vx_x, vz_z));
+        sxx = fma2(sg, fma2(M2, vx_x, tr), sxx);
+        szz = fma2(sg, fma2(M2, vz_z, tr), szz);
+        if constexpr (INTERIOR) {
+            *reinterpret_cast<float2*>(gsxx + c) = sxx;
+            *reinterpret_cast<float2*>(gszx + c) = szx;
+            *reinterpret_cast<float2*>(gszz + c) = szz;
+        } else {
+            if (fsurf && iz == FP) {
+                szz = make_float2(0.f, 0.f);
+                szx = make_float2(0.f, 0.f);
+                sxx.x = vx_x.x * (2.f * M2.x * (L.x + 0.5f * M2.x)) / (L.x + M2.x);
+                sxx.y = vx_x.y * (2.f * M2.y * (L.y + 0.5f * M2.y)) / (L.y + M2.y);
+            }
+            st2(gsxx + c, sxx, pc.on0, pc.on1);
+            st2(gszx + c, szx, pc.on0, pc.on1);
+            st2(gszz + c, szz, pc.on0, pc.on1);
+            if (fsurf && iz > FP && iz <= 2 * FP) {
+                const size_t cm = (size_t)(2 * FP - iz) * P + ix;
+                st2(gszx + cm, make_float2(-szx.x, -szx.y), pc.on0, pc.on1);
+                st2(gszz + cm, make_float2(-szz.x, -szz.y), pc.on0, pc.on1);
+            }
         }
     }
+}
+
+template <int FP>
+__device__ __forceinline__ void stress_compute(const ItemDesc& D, const TmaGrid& g, const float* st, int x0, int z0,
+                                               int it, unsigned flags, const float2 (&hx)[FP],
+                                               const float2 (&hz)[FP]) {
+    if (interior_warp(g, x0, z0, flags)) stress_rows<FP, true>(D, st, x0, z0, it, flags, hx, hz);
+    else stress_rows<FP, false>(D, st, x0, z0, it, flags, hx, hz);
 }
 
 // ---------------------------------------------------------------------------
 // velocity pass (+ energy)
 // ---------------------------------------------------------------------------
 template <int FP>
-__device__ __forceinline__ void velocity_issue(const VelMaps& m, const ItemDesc* items, const TmaGrid& g, int t,
+__device__ __forceinline__ void velocity_issue(const VelMaps& m, const ItemDesc* items, int b, int x0, int z0,
                                                float* st, uint64_t* bar, bool we) {
     using G = TmaGeom<FP>;
-    int b, x0, z0;
-    tile_coords(g, t, &b, &x0, &z0, FP);
     const unsigned bytes = 4u * (G::WX * G::TZ + G::WX * G::WZ + G::TX * G::WZ + (we ? 5 : 4) * G::CEN) +
                            (unsigned)sizeof(ItemDesc);
     mbar_expect_tx(bar, bytes);
@@ -340,38 +498,33 @@ __device__ __forceinline__ void velocity_issue(const VelMaps& m, const ItemDesc*
     if (we) tma_load_3d(c + 4 * G::CEN, &m.We, x0, z0, b, bar);
 }
 
-// Source injection and receiver recording are not done here: the engine runs
-// them in a separate small kernel after this pass (events_kernel).
-template <int FP>
-__device__ __forceinline__ void velocity_compute(const ItemDesc& D, const float* st, int x0, int z0, unsigned flags) {
+template <int FP, bool INTERIOR>
+__device__ __forceinline__ void velocity_rows(const ItemDesc& D, const float* st, int x0, int z0, unsigned flags,
+                                              const float2 (&hx)[FP], const float2 (&hz)[FP]) {
     using G = TmaGeom<FP>;
-    constexpr int R = kThreadRowsF;
-    const int tx = threadIdx.x & (kTmaTX - 1);
-    const int r0 = (threadIdx.x / kTmaTX) * R;
-    const int ix = x0 + tx;
-    const int nxt = D.nxt, nzt = D.nzt, P = D.pitch;
-    if (ix < FP || ix >= nxt - FP) return;
-    float hx[FP], hz[FP];
-#pragma unroll
-    for (int k = 0; k < FP; k++) {
-        hx[k] = D.hx[k];
-        hz[k] = D.hz[k];
+    constexpr int R = kPairRows;
+    constexpr int W = R + 2 * FP - 1;
+    const int cp = (threadIdx.x & (kTmaTX / 2 - 1)) * 2;
+    const int r0 = (threadIdx.x / (kTmaTX / 2)) * R;
+    const int ix = x0 + cp;
+    PairCols pc = {true, true, {-1, -1}};
+    if constexpr (!INTERIOR) {
+        pc = pair_cols<FP>(D, ix, false);
+        if (!pc.on0 && !pc.on1) return;
     }
-    const float* ssxx = st;                       // [TZ][WX]
-    const float* sszx = st + G::HXO;              // [WZ][WX]
-    const float* sszz = st + G::HXO + G::HXZ;     // [WZ][TX]
+    const int nzt = D.nzt, P = D.pitch, tp = D.tp;
+    const float* ssxx = st;                    // [TZ][WX]
+    const float* sszx = st + G::HXO;           // [WZ][WX]
+    const float* sszz = st + G::HXO + G::HXZ;  // [WZ][TX]
     const float* cen = st + G::HXO + G::HXZ + G::HZO;
-    const int col = tx + G::HX;
-    // z-windows: wsx[j] = szx of row r0 + j - FP, wsz[j] = szz of row r0 + j - FP + 1
-    float wsx[R + 2 * FP - 1], wsz[R + 2 * FP - 1];
+    const int col = cp + G::HX;
+    // z-windows: wsx[j] = szx pair of row r0 + j - FP, wsz[j] = szz pair of row r0 + j - FP + 1
+    float2 wsx[W], wsz[W];
 #pragma unroll
-    for (int j = 0; j < R + 2 * FP - 1; j++) {
-        wsx[j] = sszx[(r0 + j) * G::WX + col];
-        wsz[j] = sszz[(r0 + j + 1) * G::TX + tx];
+    for (int j = 0; j < W; j++) {
+        wsx[j] = ld2(sszx + (r0 + j) * G::WX + col);
+        wsz[j] = ld2(sszz + (r0 + j + 1) * G::TX + cp);
     }
-    const int ppad = D.ppad, npml = D.npml, tp = D.tp, pnz = D.pnz;
-    const bool fsurf = D.fsurf != 0;
-    const float* __restrict__ cpml = D.cpml;
     float* __restrict__ gvx = D.vx;
     float* __restrict__ gvz = D.vz;
     float* __restrict__ gwe = D.We;
@@ -379,94 +532,121 @@ __device__ __forceinline__ void velocity_compute(const ItemDesc& D, const float*
     float* __restrict__ mszx_x = D.mszx_x;
     float* __restrict__ mszz_z = D.mszz_z;
     float* __restrict__ mszx_z = D.mszx_z;
-    int px = -1;
-    if (npml > 0) {
-        if (ix < ppad) px = ix - FP;
-        else if (ix >= nxt - ppad - 1) px = ix - D.pnx;
-        if (px == npml) px = -1;
-    }
-    Cpml cx = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    if (px >= 0) cx = load_cpml(cpml, tp, px);
-    float mx1[R], mx2[R], mz1[R], mz2[R];
+    float mx1[R][2], mx2[R][2];
+    float2 mz1[R], mz2[R];
     int pzr[R];
+    if constexpr (!INTERIOR) {
 #pragma unroll
-    for (int rr = 0; rr < R; rr++) {
-        const int iz = z0 + r0 + rr;
-        mx1[rr] = mx2[rr] = mz1[rr] = mz2[rr] = 0.f;
-        int pz = -1;
-        if (npml > 0 && iz < nzt - FP) {
-            if (!fsurf && iz < ppad) pz = iz - FP;
-            else if (iz >= nzt - ppad - 1) pz = iz - pnz;
-            if (pz == npml) pz = -1;
-        }
-        pzr[rr] = pz;
-        if (px >= 0 && iz < nzt - FP) {
-            mx1[rr] = msxx_x[(size_t)iz * tp + px];
-            mx2[rr] = mszx_x[(size_t)iz * tp + px];
-        }
-        if (pz >= 0) {
-            mz1[rr] = mszz_z[(size_t)pz * P + ix];
-            mz2[rr] = mszx_z[(size_t)pz * P + ix];
+        for (int rr = 0; rr < R; rr++) {
+            const int iz = z0 + r0 + rr;
+            mz1[rr] = mz2[rr] = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int l = 0; l < 2; l++) {
+                mx1[rr][l] = mx2[rr][l] = 0.f;
+                if (pc.px[l] >= 0 && iz < nzt - FP) {
+                    mx1[rr][l] = msxx_x[(size_t)iz * tp + pc.px[l]];
+                    mx2[rr][l] = mszx_x[(size_t)iz * tp + pc.px[l]];
+                }
+            }
+            pzr[rr] = strip_z<FP>(D, iz, false);
+            if (pzr[rr] >= 0) {
+                mz1[rr] = ld2(mszz_z + (size_t)pzr[rr] * P + ix);
+                mz2[rr] = ld2(mszx_z + (size_t)pzr[rr] * P + ix);
+            }
         }
     }
     const bool we = (flags & FL_WE) != 0;
-    const float sg = (flags & FL_REVERSE) ? -1.f : 1.f;  // v^n = v^{n+1} - V(s^{n+1})
+    const float2 sg = bc2((flags & FL_REVERSE) ? -1.f : 1.f);  // v^n = v^{n+1} - V(s^{n+1})
+    size_t c = (size_t)(z0 + r0) * P + ix;
 #pragma unroll
-    for (int rr = 0; rr < R; rr++) {
+    for (int rr = 0; rr < R; rr++, c += P) {
         const int r = r0 + rr;
         const int iz = z0 + r;
-        if (iz >= nzt - FP) break;
-        const float* sxr = ssxx + r * G::WX + col;
-        const float* szr = sszx + (r + FP) * G::WX + col;
-        float sxx_x = 0.f, szx_x = 0.f, szx_z = 0.f, szz_z = 0.f;
+        if constexpr (!INTERIOR) {
+            if (iz >= nzt - FP) break;
+        }
+        RowPairs<FP> tsx, tzx;
+        // sxx has no z halo: its centre pair is not in a window
+        tsx.load(ssxx + r * G::WX + col, ld2(ssxx + r * G::WX + col));
+        tzx.load(sszx + (r + FP) * G::WX + col, wsx[rr + FP]);
+        float2 sxx_x = tsx.dplus(hx);
+        float2 szx_x = tzx.dminus(hx);
+        float2 szx_z = make_float2(0.f, 0.f), szz_z = make_float2(0.f, 0.f);
 #pragma unroll
         for (int k = 1; k <= FP; k++) {
-            sxx_x += hx[k - 1] * (sxr[k] - sxr[-k + 1]);
-            szx_x += hx[k - 1] * ((k == 1 ? wsx[rr + FP] : szr[k - 1]) - szr[-k]);
-            szx_z += hz[k - 1] * (wsx[rr + k - 1 + FP] - wsx[rr - k + FP]);
-            szz_z += hz[k - 1] * (wsz[rr + k + FP - 1] - wsz[rr - k + FP]);
+            szx_z = fma2(hz[k - 1], sub2(wsx[rr + k - 1 + FP], wsx[rr - k + FP]), szx_z);
+            szz_z = fma2(hz[k - 1], sub2(wsz[rr + k + FP - 1], wsz[rr - k + FP]), szz_z);
         }
-        if (px >= 0) {
-            const size_t m = (size_t)iz * tp + px;
-            const float m1 = cx.b * mx1[rr] + cx.a * sxx_x;
-            const float m2 = cx.bh * mx2[rr] + cx.ah * szx_x;
-            msxx_x[m] = m1;
-            mszx_x[m] = m2;
-            sxx_x = sxx_x * cx.iK + m1;
-            szx_x = szx_x * cx.iKh + m2;
+        if constexpr (!INTERIOR) {
+            cpml_x_pair(pc, D.cpml, iz, tp, mx1[rr], mx2[rr], msxx_x, mszx_x, sxx_x, szx_x);
+            if (pzr[rr] >= 0) {
+                const Cpml cz = load_cpml(D.cpml, tp, pzr[rr]);
+                const size_t m = (size_t)pzr[rr] * P + ix;
+                const float2 m1 = fma2(bc2(cz.b), mz1[rr], mul2(bc2(cz.a), szz_z));
+                const float2 m2 = fma2(bc2(cz.bh), mz2[rr], mul2(bc2(cz.ah), szx_z));
+                st2(mszz_z + m, m1, pc.on0, pc.on1);
+                st2(mszx_z + m, m2, pc.on0, pc.on1);
+                szz_z = fma2(szz_z, bc2(cz.iK), m1);
+                szx_z = fma2(szx_z, bc2(cz.iKh), m2);
+            }
         }
-        if (pzr[rr] >= 0) {
-            const int pz = pzr[rr];
-            const Cpml cz = load_cpml(cpml, tp, pz);
-            const size_t m = (size_t)pz * P + ix;
-            const float m1 = cz.b * mz1[rr] + cz.a * szz_z;
-            const float m2 = cz.bh * mz2[rr] + cz.ah * szx_z;
-            mszz_z[m] = m1;
-            mszx_z[m] = m2;
-            szz_z = szz_z * cz.iK + m1;
-            szx_z = szx_z * cz.iKh + m2;
+        const int ci = r * kTmaTX + cp;
+        const float2 vxn = fma2(sg, mul2(ld2(cen + ci), add2(sxx_x, szx_z)), ld2(cen + 2 * G::CEN + ci));
+        const float2 vzn = fma2(sg, mul2(ld2(cen + G::CEN + ci), add2(szx_x, szz_z)), ld2(cen + 3 * G::CEN + ci));
+        if constexpr (INTERIOR) {
+            if (we)
+                *reinterpret_cast<float2*>(gwe + c) = add2(ld2(cen + 4 * G::CEN + ci), fma2(vxn, vxn, mul2(vzn, vzn)));
+            *reinterpret_cast<float2*>(gvx + c) = vxn;
+            *reinterpret_cast<float2*>(gvz + c) = vzn;
+        } else {
+            if (we) st2(gwe + c, add2(ld2(cen + 4 * G::CEN + ci), fma2(vxn, vxn, mul2(vzn, vzn))), pc.on0, pc.on1);
+            st2(gvx + c, vxn, pc.on0, pc.on1);
+            st2(gvz + c, vzn, pc.on0, pc.on1);
         }
-        const int ci = r * kTmaTX + tx;
-        const float vxn = cen[2 * G::CEN + ci] + sg * (cen[ci] * (sxx_x + szx_z));
-        const float vzn = cen[3 * G::CEN + ci] + sg * (cen[G::CEN + ci] * (szx_x + szz_z));
-        const size_t c = (size_t)iz * P + ix;
-        if (we) gwe[c] = cen[4 * G::CEN + ci] + (vxn * vxn + vzn * vzn);
-        gvx[c] = vxn;
-        gvz[c] = vzn;
+    }
+}
+
+// Source injection and receiver recording are not done here: the engine runs
+// them in a separate small kernel after this pass (events_kernel).
+template <int FP>
+__device__ __forceinline__ void velocity_compute(const ItemDesc& D, const TmaGrid& g, const float* st, int x0,
+                                                 int z0, unsigned flags, const float2 (&hx)[FP],
+                                                 const float2 (&hz)[FP]) {
+    if (interior_warp(g, x0, z0, flags)) velocity_rows<FP, true>(D, st, x0, z0, flags, hx, hz);
+    else velocity_rows<FP, false>(D, st, x0, z0, flags, hx, hz);
+}
+
+// Stencil weights of a launch (every slot of a launch has the same grid),
+// read once per CTA and held in registers as broadcast pairs.
+template <int FP>
+__device__ __forceinline__ void load_weights(const ItemDesc* items, float2 (&hx)[FP], float2 (&hz)[FP]) {
+#pragma unroll
+    for (int k = 0; k < FP; k++) {
+        hx[k] = bc2(__ldg(&items[0].hx[k]));
+        hz[k] = bc2(__ldg(&items[0].hz[k]));
     }
 }
 
 // ---------------------------------------------------------------------------
 // persistent pipelined kernels
 // ---------------------------------------------------------------------------
-// Body shared by the passes.  ISSUE(t, stage_ptr, bar) queues the copies of
-// tile t; COMPUTE(b, x0, z0, stage_ptr) runs the cells; TZ is the tile height.
+// Body shared by the passes.  ISSUE(b, x0, z0, stage_ptr, bar) queues the
+// copies of a tile; COMPUTE(b, x0, z0, stage_ptr) runs its cells; TZ is the
+// tile height.  The issuing thread writes each tile's coordinates beside the
+// barriers, so the other threads do no integer division per tile.
+template <int STAGES>
+__host__ __device__ constexpr size_t tma_tail_bytes() {
+    return STAGES * (sizeof(int4) + sizeof(uint64_t));
+}
+
 template <int FP, int STAGE_FLOATS, int TZ, class Issue, class Compute>
 __device__ __forceinline__ void tma_pipeline(const TmaGrid& g, int* err, Issue issue, Compute compute) {
     constexpr int kTmaStages = tma_stages<FP>();
-    // dynamic shared memory only: the stages (128-byte multiples) then the barriers
+    static_assert(STAGE_FLOATS % 32 == 0, "stages are 128-byte multiples");
+    // dynamic shared memory only: the stages, the tile coordinates, the barriers
     extern __shared__ __align__(128) float tma_smem[];
-    uint64_t* bar = reinterpret_cast<uint64_t*>(tma_smem + kTmaStages * STAGE_FLOATS);
+    int4* crd = reinterpret_cast<int4*>(tma_smem + kTmaStages * STAGE_FLOATS);
+    uint64_t* bar = reinterpret_cast<uint64_t*>(crd + kTmaStages);
     const int tid = threadIdx.x;
     // an earlier launch gave up (error word set): return at once, so a failing
     // pipeline costs one bounded wait and not one per launch; the decision is
@@ -476,26 +656,32 @@ __device__ __forceinline__ void tma_pipeline(const TmaGrid& g, int* err, Issue i
         if (tid == 0) atomicOr(err, 8);
         return;
     }
+    const int first = blockIdx.x, step = gridDim.x;
+    auto issue_tile = [&](int t, int s) {
+        int b, x0, z0;
+        tile_coords(g, t, &b, &x0, &z0, FP, TZ);
+        crd[s] = make_int4(b, x0, z0, 0);
+        issue(b, x0, z0, tma_smem + s * STAGE_FLOATS, &bar[s]);
+    };
     if (tid == 0) {
         for (int s = 0; s < kTmaStages; s++) mbar_init(&bar[s], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    }
-    __syncthreads();
-    const int first = blockIdx.x, step = gridDim.x;
-    if (tid == 0)
         for (int s = 0; s < kTmaStages; s++) {
             const int t = first + s * step;
-            if (t < g.ntiles) issue(t, tma_smem + s * STAGE_FLOATS, &bar[s]);
+            if (t < g.ntiles) issue_tile(t, s);
         }
+    }
+    __syncthreads();
     for (int k = 0;; k++) {
         const int t = first + k * step;
         if (t >= g.ntiles) break;
         const int s = k % kTmaStages;
         const unsigned parity = (unsigned)((k / kTmaStages) & 1);
         const bool ok = mbar_wait_bounded(&bar[s], parity);
-        int b, x0, z0;
-        tile_coords(g, t, &b, &x0, &z0, FP, TZ);
-        if (ok) compute(b, x0, z0, tma_smem + s * STAGE_FLOATS);
+        if (ok) {
+            const int4 c = crd[s];
+            compute(c.x, c.y, c.z, tma_smem + s * STAGE_FLOATS);
+        }
         // every thread is done with stage s (or some thread's wait gave up)
         if (__syncthreads_or(!ok)) {
             if (tid == 0) {
@@ -512,7 +698,7 @@ __device__ __forceinline__ void tma_pipeline(const TmaGrid& g, int* err, Issue i
             const int tn = first + (k + kTmaStages) * step;
             if (tn < g.ntiles) {
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                issue(tn, tma_smem + s * STAGE_FLOATS, &bar[s]);
+                issue_tile(tn, s);
             }
         }
     }
@@ -520,11 +706,11 @@ __device__ __forceinline__ void tma_pipeline(const TmaGrid& g, int* err, Issue i
 
 template <int FP>
 constexpr size_t stress_tma_smem() {
-    return sizeof(float) * tma_stages<FP>() * TmaGeom<FP>::S_STAGE + sizeof(uint64_t) * tma_stages<FP>();
+    return sizeof(float) * tma_stages<FP>() * TmaGeom<FP>::S_STAGE + tma_tail_bytes<tma_stages<FP>()>();
 }
 template <int FP>
 constexpr size_t velocity_tma_smem() {
-    return sizeof(float) * tma_stages<FP>() * TmaGeom<FP>::V_STAGE + sizeof(uint64_t) * tma_stages<FP>();
+    return sizeof(float) * tma_stages<FP>() * TmaGeom<FP>::V_STAGE + tma_tail_bytes<tma_stages<FP>()>();
 }
 static_assert(stress_tma_smem<4>() <= 232448 && velocity_tma_smem<4>() <= 232448, "shared memory per CTA");
 static_assert(stress_tma_smem<6>() <= 232448 && velocity_tma_smem<6>() <= 232448, "shared memory per CTA");
@@ -534,10 +720,14 @@ __global__ void __launch_bounds__(kTmaThreads, 1)
     stress_tma_kernel(const __grid_constant__ StressMaps maps, const ItemDesc* __restrict__ items,
                       const TmaGrid g, int it, unsigned flags, int* err) {
     using G = TmaGeom<FP>;
+    float2 hx[FP], hz[FP];
+    load_weights<FP>(items, hx, hz);
     tma_pipeline<FP, G::S_STAGE, kTmaTZ>(
-        g, err, [&](int t, float* st, uint64_t* bar) { stress_issue<FP>(maps, items, g, t, st, bar); },
+        g, err,
+        [&](int b, int x0, int z0, float* st, uint64_t* bar) { stress_issue<FP>(maps, items, b, x0, z0, st, bar); },
         [&](int, int x0, int z0, const float* st) {
-            stress_compute<FP>(*reinterpret_cast<const ItemDesc*>(st + G::S_DESC), st, x0, z0, it, flags);
+            stress_compute<FP>(*reinterpret_cast<const ItemDesc*>(st + G::S_DESC), g, st, x0, z0, it, flags, hx,
+                               hz);
         });
 }
 
@@ -547,13 +737,17 @@ __global__ void __launch_bounds__(kTmaThreads, 1)
                         const TmaGrid g, int it, unsigned flags, int* err) {
     using G = TmaGeom<FP>;
     const bool we = (flags & FL_WE) != 0;
+    float2 hx[FP], hz[FP];
+    load_weights<FP>(items, hx, hz);
     tma_pipeline<FP, G::V_STAGE, kTmaTZ>(
-        g, err, [&](int t, float* st, uint64_t* bar) { velocity_issue<FP>(maps, items, g, t, st, bar, we); },
+        g, err,
+        [&](int b, int x0, int z0, float* st, uint64_t* bar) {
+            velocity_issue<FP>(maps, items, b, x0, z0, st, bar, we);
+        },
         [&](int, int x0, int z0, const float* st) {
-            velocity_compute<FP>(*reinterpret_cast<const ItemDesc*>(st + G::V_DESC), st, x0, z0, flags);
+            velocity_compute<FP>(*reinterpret_cast<const ItemDesc*>(st + G::V_DESC), g, st, x0, z0, flags, hx, hz);
         });
 }
-
 
 // ---------------------------------------------------------------------------
 // adjoint stress pass with the reference's gradient (128 x 8 tiles)
@@ -584,16 +778,14 @@ struct AdjMaps {
 
 template <int FP>
 __host__ __device__ constexpr size_t adjoint_tma_smem() {
-    return sizeof(float) * tma_stages<FP>() * AdjGeom<FP>::STAGE + sizeof(uint64_t) * tma_stages<FP>();
+    return sizeof(float) * tma_stages<FP>() * AdjGeom<FP>::STAGE + tma_tail_bytes<tma_stages<FP>()>();
 }
 static_assert(adjoint_tma_smem<4>() <= 232448 && adjoint_tma_smem<6>() <= 232448, "shared memory per CTA");
 
 template <int FP>
-__device__ __forceinline__ void adjoint_issue(const AdjMaps& m, const ItemDesc* items, const TmaGrid& g, int t,
+__device__ __forceinline__ void adjoint_issue(const AdjMaps& m, const ItemDesc* items, int b, int x0, int z0,
                                               float* st, uint64_t* bar, bool grad) {
     using G = AdjGeom<FP>;
-    int b, x0, z0;
-    tile_coords(g, t, &b, &x0, &z0, FP, kAdjTZ);
     const unsigned bytes = 4u * (2 * G::WX * G::WZ + (grad ? 13 : 8) * G::CEN) + (unsigned)sizeof(ItemDesc);
     mbar_expect_tx(bar, bytes);
     bulk_load(st + G::DESC, items + b, (unsigned)sizeof(ItemDesc), bar);
@@ -793,7 +985,10 @@ __global__ void __launch_bounds__(kTmaThreads, 1)
     using G = AdjGeom<FP>;
     const bool grad = (flags & FL_GRAD) != 0;
     tma_pipeline<FP, G::STAGE, kAdjTZ>(
-        g, err, [&](int t, float* st, uint64_t* bar) { adjoint_issue<FP>(maps, items, g, t, st, bar, grad); },
+        g, err,
+        [&](int b, int x0, int z0, float* st, uint64_t* bar) {
+            adjoint_issue<FP>(maps, items, b, x0, z0, st, bar, grad);
+        },
         [&](int, int x0, int z0, const float* st) {
             adjoint_compute<FP>(*reinterpret_cast<const ItemDesc*>(st + G::DESC), st, x0, z0, it, grad);
         });
