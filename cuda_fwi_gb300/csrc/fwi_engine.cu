@@ -1121,6 +1121,14 @@ struct Engine {
             if (!fsurf) tgrid.czl = std::max(tgrid.czl, ppad + 1);
         }
         if (fsurf) tgrid.czl = std::max(tgrid.czl, 2 * fpad + 1);
+        tgrid.gxl = tgrid.gzl = 0;
+        tgrid.gxh = tgrid.gzh = -1;
+        if (fwi_dx == 1 && fwi_dz == 1) {
+            tgrid.gxl = wx1;
+            tgrid.gxh = wx2 - 1;
+            tgrid.gzl = wz1;
+            tgrid.gzh = wz2 - 1;
+        }
         grid_tma = std::max(1, std::min(tgrid.ntiles, num_sms));
         const int ntz_a = (nzt - 2 * fpad + kAdjTZ - 1) / kAdjTZ;
         tgrid_a = tgrid;

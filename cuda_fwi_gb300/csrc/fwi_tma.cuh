@@ -78,9 +78,12 @@ struct VelMaps {
 // [cxl, cxh] x [czl, czh] (inclusive) are the cells that both forward passes
 // update with the plain stencil: no border column, no CPML strip (taken one
 // cell wider than either pass uses it), no free-surface row or mirror row.
+// [gxl, gxh] x [gzl, gzh]: the gradient window when it is sampled at unit
+// intervals (empty otherwise).
 struct TmaGrid {
     int nb, ntz, ntiles, pad;
     int cxl, cxh, czl, czh;
+    int gxl, gxh, gzl, gzh;
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -631,9 +634,11 @@ __device__ __forceinline__ void load_weights(const ItemDesc* items, float2 (&hx)
 // persistent pipelined kernels
 // ---------------------------------------------------------------------------
 // Body shared by the passes.  ISSUE(b, x0, z0, stage_ptr, bar) queues the
-// copies of a tile; COMPUTE(b, x0, z0, stage_ptr) runs its cells; TZ is the
-// tile height.  The issuing thread writes each tile's coordinates beside the
-// barriers, so the other threads do no integer division per tile.
+// copies of a tile; COMPUTE(tile, next, stage_ptr) runs its cells (tile and
+// next are (b, x0, z0) of this tile and of the CTA's next one, b = -1 when
+// there is none); TZ is the tile height.  The issuing thread writes each
+// tile's coordinates beside the barriers, so the other threads do no integer
+// division per tile.
 template <int STAGES>
 __host__ __device__ constexpr size_t tma_tail_bytes() {
     return STAGES * (sizeof(int4) + sizeof(uint64_t));
@@ -679,8 +684,9 @@ __device__ __forceinline__ void tma_pipeline(const TmaGrid& g, int* err, Issue i
         const unsigned parity = (unsigned)((k / kTmaStages) & 1);
         const bool ok = mbar_wait_bounded(&bar[s], parity);
         if (ok) {
-            const int4 c = crd[s];
-            compute(c.x, c.y, c.z, tma_smem + s * STAGE_FLOATS);
+            // coordinates of this thread's next tile (issued already: stages >= 2)
+            const int4 nx = first + (k + 1) * step < g.ntiles ? crd[(k + 1) % kTmaStages] : make_int4(-1, 0, 0, 0);
+            compute(crd[s], nx, tma_smem + s * STAGE_FLOATS);
         }
         // every thread is done with stage s (or some thread's wait gave up)
         if (__syncthreads_or(!ok)) {
@@ -725,8 +731,8 @@ __global__ void __launch_bounds__(kTmaThreads, 1)
     tma_pipeline<FP, G::S_STAGE, kTmaTZ>(
         g, err,
         [&](int b, int x0, int z0, float* st, uint64_t* bar) { stress_issue<FP>(maps, items, b, x0, z0, st, bar); },
-        [&](int, int x0, int z0, const float* st) {
-            stress_compute<FP>(*reinterpret_cast<const ItemDesc*>(st + G::S_DESC), g, st, x0, z0, it, flags, hx,
+        [&](int4 c, int4, const float* st) {
+            stress_compute<FP>(*reinterpret_cast<const ItemDesc*>(st + G::S_DESC), g, st, c.y, c.z, it, flags, hx,
                                hz);
         });
 }
@@ -744,8 +750,8 @@ __global__ void __launch_bounds__(kTmaThreads, 1)
         [&](int b, int x0, int z0, float* st, uint64_t* bar) {
             velocity_issue<FP>(maps, items, b, x0, z0, st, bar, we);
         },
-        [&](int, int x0, int z0, const float* st) {
-            velocity_compute<FP>(*reinterpret_cast<const ItemDesc*>(st + G::V_DESC), g, st, x0, z0, flags, hx, hz);
+        [&](int4 c, int4, const float* st) {
+            velocity_compute<FP>(*reinterpret_cast<const ItemDesc*>(st + G::V_DESC), g, st, c.y, c.z, flags, hx, hz);
         });
 }
 
@@ -809,171 +815,202 @@ __device__ __forceinline__ void adjoint_issue(const AdjMaps& m, const ItemDesc* 
     }
 }
 
-template <int FP>
-__device__ __forceinline__ void adjoint_compute(const ItemDesc& D, const float* st, int x0, int z0, int it,
-                                                bool grad_step) {
+// The adjoint pass maps a column pair to each thread and one tile row
+// (64 pairs x 8 rows); warp w covers 64 columns of tile row w / 2.
+static_assert((kTmaTX / 2) * kAdjTZ == kTmaThreads, "one thread per column pair of a row");
+
+// The warp's cells are plain-stencil cells and, on a gradient step, lie in
+// the gradient window sampled at unit intervals.
+__device__ __forceinline__ bool interior_warp_adj(const TmaGrid& g, int x0, int z0, bool grad_step) {
+    const int w = threadIdx.x >> 5;
+    const int wx0 = x0 + (w & 1) * 64, wz = z0 + (w >> 1);
+    bool in = wx0 >= g.cxl && wx0 + 63 <= g.cxh && wz >= g.czl && wz <= g.czh;
+    if (grad_step) in = in && wx0 >= g.gxl && wx0 + 63 <= g.gxh && wz >= g.gzl && wz <= g.gzh;
+    return in;
+}
+
+__device__ __forceinline__ float* ldg_ptr(float* const* p) {
+    return reinterpret_cast<float*>(__ldg(reinterpret_cast<const unsigned long long*>(p)));
+}
+
+// Gradient samples of an interior warp's pair loaded one tile ahead: the
+// loads are issued at the end of the previous tile, so their DRAM latency
+// passes while the CTA waits for and computes the current one.
+struct GradAhead {
+    float g[6];  // lam, mu, rho of the two columns
+    bool valid;
+};
+
+template <int FP, bool INTERIOR>
+__device__ __forceinline__ void adjoint_rows(const ItemDesc& D, const float* st, int x0, int z0, bool grad_step,
+                                             const float2 (&hx)[FP], const float2 (&hz)[FP], const GradAhead& ga) {
     using G = AdjGeom<FP>;
-    constexpr int R = kAdjTZ / (kTmaThreads / kTmaTX);
-    const int tx = threadIdx.x & (kTmaTX - 1);
-    const int r0 = (threadIdx.x / kTmaTX) * R;
-    const int ix = x0 + tx;
-    const int nxt = D.nxt, nzt = D.nzt, P = D.pitch;
-    if (ix < FP || ix >= nxt - FP) return;
-    float hx[FP], hz[FP];
+    const int cp = (threadIdx.x & (kTmaTX / 2 - 1)) * 2;
+    const int r = threadIdx.x / (kTmaTX / 2);  // tile row
+    const int ix = x0 + cp, iz = z0 + r;
+    const int P = D.pitch, tp = D.tp;
+    PairCols pc = {true, true, {-1, -1}};
+    if constexpr (!INTERIOR) {
+        if (iz >= D.nzt - FP) return;
+        pc = pair_cols<FP>(D, ix, true);
+        if (!pc.on0 && !pc.on1) return;
+    }
+    const size_t c = (size_t)iz * P + ix;
+    // gradient samples of the pair (prefetched: their loads overlap the stencil)
+    int gi[2] = {-1, -1};
+    float g0[2] = {0.f, 0.f}, g1[2] = {0.f, 0.f}, g2[2] = {0.f, 0.f};
+    float* __restrict__ glam = D.glam;
+    float* __restrict__ gmu = D.gmu;
+    float* __restrict__ grho = D.grho;
+    if (grad_step) {
+        if constexpr (INTERIOR) {
+            gi[0] = (iz - D.wz1) * D.nfx + (ix - D.wx1);
+            gi[1] = gi[0] + 1;
+        } else {
+            const int dzw = iz - D.wz1;
+            if (iz >= D.wz1 && iz < D.wz2 && (D.fwi_dz == 1 || dzw % D.fwi_dz == 0)) {
+                const int zf = D.fwi_dz == 1 ? dzw : dzw / D.fwi_dz;
 #pragma unroll
-    for (int k = 0; k < FP; k++) {
-        hx[k] = D.hx[k];
-        hz[k] = D.hz[k];
+                for (int l = 0; l < 2; l++) {
+                    const int dxw = ix + l - D.wx1;
+                    if ((l ? pc.on1 : pc.on0) && dxw >= 0 && ix + l < D.wx2 && (D.fwi_dx == 1 || dxw % D.fwi_dx == 0))
+                        gi[l] = zf * D.nfx + (D.fwi_dx == 1 ? dxw : dxw / D.fwi_dx);
+                }
+            }
+        }
+        if (INTERIOR && ga.valid) {
+#pragma unroll
+            for (int l = 0; l < 2; l++) {
+                g0[l] = ga.g[l];
+                g1[l] = ga.g[2 + l];
+                g2[l] = ga.g[4 + l];
+            }
+        } else {
+#pragma unroll
+            for (int l = 0; l < 2; l++) {
+                if (gi[l] >= 0) {
+                    g0[l] = glam[gi[l]];
+                    g1[l] = gmu[gi[l]];
+                    g2[l] = grho[gi[l]];
+                }
+            }
+        }
+    }
+    // CPML memories of the pair
+    float mx1[2] = {0.f, 0.f}, mx2[2] = {0.f, 0.f};
+    float2 mz1 = make_float2(0.f, 0.f), mz2 = make_float2(0.f, 0.f);
+    int pz = -1;
+    if constexpr (!INTERIOR) {
+#pragma unroll
+        for (int l = 0; l < 2; l++) {
+            if (pc.px[l] >= 0) {
+                mx1[l] = D.mvx_x[(size_t)iz * tp + pc.px[l]];
+                mx2[l] = D.mvz_x[(size_t)iz * tp + pc.px[l]];
+            }
+        }
+        pz = strip_z<FP>(D, iz, true);
+        if (pz >= 0) {
+            mz1 = ld2(D.mvz_z + (size_t)pz * P + ix);
+            mz2 = ld2(D.mvx_z + (size_t)pz * P + ix);
+        }
     }
     const float* svx = st;
     const float* svz = st + G::HXZ;
     const float* cen = st + 2 * G::HXZ;
-    const int col = tx + G::HX;
-    float wvx[R + 2 * FP - 1], wvz[R + 2 * FP - 1];
+    const int col = cp + G::HX;
+    const int row = r + FP;
+    const float2 cvx = ld2(svx + row * G::WX + col), cvz = ld2(svz + row * G::WX + col);
+    RowPairs<FP> tvx, tvz;
+    tvx.load(svx + row * G::WX + col, cvx);
+    tvz.load(svz + row * G::WX + col, cvz);
+    float2 vx_x = tvx.dminus(hx);
+    float2 vz_x = tvz.dplus(hx);
+    // z taps straight from the stage: vx D+ (rows r+k, r-k+1), vz D- (rows r+k-1, r-k)
+    float2 vx_z = make_float2(0.f, 0.f), vz_z = make_float2(0.f, 0.f);
 #pragma unroll
-    for (int j = 0; j < R + 2 * FP - 1; j++) {
-        wvx[j] = svx[(r0 + j + 1) * G::WX + col];
-        wvz[j] = svz[(r0 + j) * G::WX + col];
+    for (int k = 1; k <= FP; k++) {
+        const float2 a = ld2(svx + (row + k) * G::WX + col);
+        const float2 bb = k == 1 ? cvx : ld2(svx + (row - k + 1) * G::WX + col);
+        const float2 e = k == 1 ? cvz : ld2(svz + (row + k - 1) * G::WX + col);
+        const float2 f = ld2(svz + (row - k) * G::WX + col);
+        vx_z = fma2(hz[k - 1], sub2(a, bb), vx_z);
+        vz_z = fma2(hz[k - 1], sub2(e, f), vz_z);
     }
-    const float dt = D.dt, inv_dt = D.inv_dt, gs = D.gscale;
-    const int ppad = D.ppad, npml = D.npml, tp = D.tp, pnz = D.pnz;
-    const bool fsurf = D.fsurf != 0;
-    const float* __restrict__ cpml = D.cpml;
-    float* __restrict__ gsxx = D.sxx;
-    float* __restrict__ gszx = D.szx;
-    float* __restrict__ gszz = D.szz;
-    float* __restrict__ gux = D.ux;
-    float* __restrict__ guz = D.uz;
-    float* __restrict__ mvx_x = D.mvx_x;
-    float* __restrict__ mvz_x = D.mvz_x;
-    float* __restrict__ mvx_z = D.mvx_z;
-    float* __restrict__ mvz_z = D.mvz_z;
-    int px = -1;
-    if (npml > 0) {
-        if (ix <= ppad) px = ix - FP;
-        else if (ix >= nxt - ppad - 1) px = ix - D.pnx;
-        if (px == npml) px = -1;
-    }
-    Cpml cx = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    if (px >= 0) cx = load_cpml(cpml, tp, px);
-    // gradient window column of this thread
-    int xf = -1;
-    const int wz1 = D.wz1, wz2 = D.wz2, fdz = D.fwi_dz, nfx = D.nfx;
-    if (grad_step && ix >= D.wx1 && ix < D.wx2) {
-        // unit intervals (the common case) need no integer division
-        const int dxw = ix - D.wx1;
-        if (D.fwi_dx == 1) xf = dxw;
-        else if (dxw % D.fwi_dx == 0) xf = dxw / D.fwi_dx;
-    }
-    float* __restrict__ glam = D.glam;
-    float* __restrict__ gmu = D.gmu;
-    float* __restrict__ grho = D.grho;
-    float mx1[R], mx2[R], mz1[R], mz2[R], g0[R], g1[R], g2[R];
-    int pzr[R], gi[R];
-#pragma unroll
-    for (int rr = 0; rr < R; rr++) {
-        const int iz = z0 + r0 + rr;
-        mx1[rr] = mx2[rr] = mz1[rr] = mz2[rr] = g0[rr] = g1[rr] = g2[rr] = 0.f;
-        int pz = -1;
-        if (npml > 0 && iz < nzt - FP) {
-            if (!fsurf && iz <= ppad) pz = iz - FP;
-            else if (iz >= nzt - ppad - 1) pz = iz - pnz;
-            if (pz == npml) pz = -1;
-        }
-        pzr[rr] = pz;
-        if (px >= 0 && iz < nzt - FP) {
-            mx1[rr] = mvx_x[(size_t)iz * tp + px];
-            mx2[rr] = mvz_x[(size_t)iz * tp + px];
-        }
+    if constexpr (!INTERIOR) {
+        cpml_x_pair(pc, D.cpml, iz, tp, mx1, mx2, D.mvx_x, D.mvz_x, vx_x, vz_x);
         if (pz >= 0) {
-            mz1[rr] = mvz_z[(size_t)pz * P + ix];
-            mz2[rr] = mvx_z[(size_t)pz * P + ix];
-        }
-        gi[rr] = -1;
-        if (xf >= 0 && iz < nzt - FP && iz >= wz1 && iz < wz2 && (fdz == 1 || (iz - wz1) % fdz == 0)) {
-            gi[rr] = (fdz == 1 ? iz - wz1 : (iz - wz1) / fdz) * nfx + xf;
-            g0[rr] = glam[gi[rr]];
-            g1[rr] = gmu[gi[rr]];
-            g2[rr] = grho[gi[rr]];
+            const Cpml cz = load_cpml(D.cpml, tp, pz);
+            const size_t m = (size_t)pz * P + ix;
+            const float2 m1 = fma2(bc2(cz.b), mz1, mul2(bc2(cz.a), vz_z));
+            const float2 m2 = fma2(bc2(cz.bh), mz2, mul2(bc2(cz.ah), vx_z));
+            st2(D.mvz_z + m, m1, pc.on0, pc.on1);
+            st2(D.mvx_z + m, m2, pc.on0, pc.on1);
+            vz_z = fma2(vz_z, bc2(cz.iK), m1);
+            vx_z = fma2(vx_z, bc2(cz.iKh), m2);
         }
     }
+    const int ci = r * kTmaTX + cp;
+    const float2 L = ld2(cen + ci), M2 = ld2(cen + G::CEN + ci), MZ = ld2(cen + 2 * G::CEN + ci);
+    float2 sxx = ld2(cen + 3 * G::CEN + ci), szx = ld2(cen + 4 * G::CEN + ci), szz = ld2(cen + 5 * G::CEN + ci);
+    const float2 dt2 = bc2(D.dt);
+    const float2 ux = fma2(dt2, cvx, ld2(cen + 6 * G::CEN + ci));
+    const float2 uz = fma2(dt2, cvz, ld2(cen + 7 * G::CEN + ci));
+    if (gi[0] >= 0 || gi[1] >= 0) {
+        // the stored velocities are v/dt; correctly rounded reciprocals in place
+        // of the divisions (rounding within the gradient tolerance)
+        const float2 idt = bc2(D.inv_dt);
+        const float2 fvx = mul2(ld2(cen + 8 * G::CEN + ci), idt), fvz = mul2(ld2(cen + 9 * G::CEN + ci), idt);
+        const float2 fsxx = ld2(cen + 10 * G::CEN + ci), fszx = ld2(cen + 11 * G::CEN + ci);
+        const float2 fszz = ld2(cen + 12 * G::CEN + ci);
+        const float2 lpm = mul2(fma2(bc2(0.5f), M2, L), idt);
+        const float2 mu = mul2(mul2(bc2(0.5f), M2), idt);
+        const float2 lpm2 = mul2(lpm, lpm), mu2 = mul2(mu, mu);
+        const float2 ilpm2 = make_float2(0.25f * __frcp_rn(lpm2.x), 0.25f * __frcp_rn(lpm2.y));
+        const float2 imu2 = make_float2(__frcp_rn(mu2.x), __frcp_rn(mu2.y));
+        const float2 s1 = mul2(mul2(add2(fsxx, fszz), add2(sxx, szz)), ilpm2);
+        const float2 s2 = mul2(mul2(sub2(fsxx, fszz), sub2(sxx, szz)), imu2);
+        const float2 s3 = mul2(mul2(fszx, szx), imu2);
+        const float2 s4 = fma2(ux, fvx, mul2(uz, fvz));
+        const float2 gs = bc2(D.gscale);
+        const float2 nl = fma2(gs, s1, make_float2(g0[0], g0[1]));
+        const float2 nm = fma2(gs, add2(add2(s3, s1), s2), make_float2(g1[0], g1[1]));
+        const float2 nr = fma2(make_float2(-D.gscale, -D.gscale), s4, make_float2(g2[0], g2[1]));
 #pragma unroll
-    for (int rr = 0; rr < R; rr++) {
-        const int r = r0 + rr;
-        const int iz = z0 + r;
-        if (iz >= nzt - FP) break;
-        const int row = r + FP;
-        const float* vxr = svx + row * G::WX + col;
-        const float* vzr = svz + row * G::WX + col;
-        float vx_x = 0.f, vz_x = 0.f, vx_z = 0.f, vz_z = 0.f;
-#pragma unroll
-        for (int k = 1; k <= FP; k++) {
-            vx_x += hx[k - 1] * ((k == 1 ? wvx[rr + FP - 1] : vxr[k - 1]) - vxr[-k]);
-            vz_x += hx[k - 1] * (vzr[k] - (k == 1 ? wvz[rr + FP] : vzr[-k + 1]));
-            vx_z += hz[k - 1] * (wvx[rr + k + FP - 1] - wvx[rr - k + FP]);
-            vz_z += hz[k - 1] * (wvz[rr + k - 1 + FP] - wvz[rr - k + FP]);
+        for (int l = 0; l < 2; l++) {
+            if (gi[l] >= 0) {
+                glam[gi[l]] = lane(nl, l);
+                gmu[gi[l]] = lane(nm, l);
+                grho[gi[l]] = lane(nr, l);
+            }
         }
-        const size_t c = (size_t)iz * P + ix;
-        if (px >= 0) {
-            const size_t m = (size_t)iz * tp + px;
-            const float m1 = cx.b * mx1[rr] + cx.a * vx_x;
-            const float m2 = cx.bh * mx2[rr] + cx.ah * vz_x;
-            mvx_x[m] = m1;
-            mvz_x[m] = m2;
-            vx_x = vx_x * cx.iK + m1;
-            vz_x = vz_x * cx.iKh + m2;
-        }
-        if (pzr[rr] >= 0) {
-            const int pz = pzr[rr];
-            const Cpml cz = load_cpml(cpml, tp, pz);
-            const size_t m = (size_t)pz * P + ix;
-            const float m1 = cz.b * mz1[rr] + cz.a * vz_z;
-            const float m2 = cz.bh * mz2[rr] + cz.ah * vx_z;
-            mvz_z[m] = m1;
-            mvx_z[m] = m2;
-            vz_z = vz_z * cz.iK + m1;
-            vx_z = vx_z * cz.iKh + m2;
-        }
-        const int ci = r * kTmaTX + tx;
-        const float L = cen[ci], M2 = cen[G::CEN + ci], MZ = cen[2 * G::CEN + ci];
-        float sxx = cen[3 * G::CEN + ci], szx = cen[4 * G::CEN + ci], szz = cen[5 * G::CEN + ci];
-        const float ux = cen[6 * G::CEN + ci] + dt * wvx[rr + FP - 1];
-        const float uz = cen[7 * G::CEN + ci] + dt * wvz[rr + FP];
-        gux[c] = ux;
-        guz[c] = uz;
-        if (gi[rr] >= 0) {
-            // the stored velocities are v/dt; reciprocals computed once per cell
-            // (two divisions instead of five; rounding within the gradient tolerance)
-            const float fvx = cen[8 * G::CEN + ci] * inv_dt, fvz = cen[9 * G::CEN + ci] * inv_dt;
-            const float fsxx = cen[10 * G::CEN + ci], fszx = cen[11 * G::CEN + ci], fszz = cen[12 * G::CEN + ci];
-            const float lpm = (L + 0.5f * M2) * inv_dt;
-            const float mu = 0.5f * M2 * inv_dt;
-            const float ilpm2 = 0.25f / (lpm * lpm);
-            const float imu2 = 1.f / (mu * mu);
-            const float s1 = (fsxx + fszz) * (sxx + szz) * ilpm2;
-            const float s2 = (fsxx - fszz) * (sxx - szz) * imu2;
-            const float s3 = (fszx * szx) * imu2;
-            const float s4 = ux * fvx + uz * fvz;
-            glam[gi[rr]] = g0[rr] + gs * s1;
-            gmu[gi[rr]] = g1[rr] + gs * (s3 + s1 + s2);
-            grho[gi[rr]] = g2[rr] - gs * s4;
-        }
-        szx += MZ * (vz_x + vx_z);
-        const float tr = L * (vx_x + vz_z);
-        sxx += tr + M2 * vx_x;
-        szz += tr + M2 * vz_z;
+    }
+    szx = add2(szx, mul2(MZ, add2(vz_x, vx_z)));
+    const float2 tr = mul2(L, add2(vx_x, vz_z));
+    sxx = add2(sxx, fma2(M2, vx_x, tr));
+    szz = add2(szz, fma2(M2, vz_z, tr));
+    if constexpr (INTERIOR) {
+        *reinterpret_cast<float2*>(D.ux + c) = ux;
+        *reinterpret_cast<float2*>(D.uz + c) = uz;
+        *reinterpret_cast<float2*>(D.sxx + c) = sxx;
+        *reinterpret_cast<float2*>(D.szx + c) = szx;
+        *reinterpret_cast<float2*>(D.szz + c) = szz;
+    } else {
+        const bool fsurf = D.fsurf != 0;
         if (fsurf && iz == FP) {
-            szz = 0.f;
-            szx = 0.f;
-            sxx = vx_x * (2.f * M2 * (L + 0.5f * M2)) / (L + M2);
+            szz = make_float2(0.f, 0.f);
+            szx = make_float2(0.f, 0.f);
+            sxx.x = vx_x.x * (2.f * M2.x * (L.x + 0.5f * M2.x)) / (L.x + M2.x);
+            sxx.y = vx_x.y * (2.f * M2.y * (L.y + 0.5f * M2.y)) / (L.y + M2.y);
         }
-        gsxx[c] = sxx;
-        gszx[c] = szx;
-        gszz[c] = szz;
+        st2(D.ux + c, ux, pc.on0, pc.on1);
+        st2(D.uz + c, uz, pc.on0, pc.on1);
+        st2(D.sxx + c, sxx, pc.on0, pc.on1);
+        st2(D.szx + c, szx, pc.on0, pc.on1);
+        st2(D.szz + c, szz, pc.on0, pc.on1);
         if (fsurf && iz > FP && iz <= 2 * FP) {
             const size_t cm = (size_t)(2 * FP - iz) * P + ix;
-            gszx[cm] = -szx;
-            gszz[cm] = -szz;
+            st2(D.szx + cm, make_float2(-szx.x, -szx.y), pc.on0, pc.on1);
+            st2(D.szz + cm, make_float2(-szz.x, -szz.y), pc.on0, pc.on1);
         }
     }
 }
@@ -984,13 +1021,37 @@ __global__ void __launch_bounds__(kTmaThreads, 1)
                        int it, unsigned flags, int* err) {
     using G = AdjGeom<FP>;
     const bool grad = (flags & FL_GRAD) != 0;
+    float2 hx[FP], hz[FP];
+    load_weights<FP>(items, hx, hz);
+    // gradient window origin and row length (the same for every slot)
+    const int wx1 = __ldg(&items[0].wx1), wz1 = __ldg(&items[0].wz1), nfx = __ldg(&items[0].nfx);
+    GradAhead ga;
+    ga.valid = false;
     tma_pipeline<FP, G::STAGE, kAdjTZ>(
         g, err,
         [&](int b, int x0, int z0, float* st, uint64_t* bar) {
             adjoint_issue<FP>(maps, items, b, x0, z0, st, bar, grad);
         },
-        [&](int, int x0, int z0, const float* st) {
-            adjoint_compute<FP>(*reinterpret_cast<const ItemDesc*>(st + G::DESC), st, x0, z0, it, grad);
+        [&](int4 c, int4 n, const float* st) {
+            const ItemDesc& D = *reinterpret_cast<const ItemDesc*>(st + G::DESC);
+            if (interior_warp_adj(g, c.y, c.z, grad)) adjoint_rows<FP, true>(D, st, c.y, c.z, grad, hx, hz, ga);
+            else adjoint_rows<FP, false>(D, st, c.y, c.z, grad, hx, hz, ga);
+            ga.valid = false;
+            if (grad && n.x >= 0 && interior_warp_adj(g, n.y, n.z, true)) {
+                const ItemDesc* In = items + n.x;
+                const int gi = (n.z + (int)(threadIdx.x / (kTmaTX / 2)) - wz1) * nfx +
+                               (n.y + (int)(threadIdx.x & (kTmaTX / 2 - 1)) * 2 - wx1);
+                const float* gl = ldg_ptr(&In->glam);
+                const float* gm = ldg_ptr(&In->gmu);
+                const float* gr = ldg_ptr(&In->grho);
+                ga.g[0] = gl[gi];
+                ga.g[1] = gl[gi + 1];
+                ga.g[2] = gm[gi];
+                ga.g[3] = gm[gi + 1];
+                ga.g[4] = gr[gi];
+                ga.g[5] = gr[gi + 1];
+                ga.valid = true;
+            }
         });
 }
 
