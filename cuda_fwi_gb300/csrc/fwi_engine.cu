@@ -226,6 +226,32 @@ __global__ void precondition_kernel(const ItemDesc* __restrict__ items, const fl
     }
 }
 
+// Device copy of whole batch states (checkpoint saves and restores) on the
+// SMs: 16-byte loads and stores, four in flight per thread.  For copies of
+// this size (a 14-shot state of the 1068x568 grid is ~200 MB) the SMs move
+// about twice the bytes per second of the device-to-device copy engines.
+__global__ void copy_kernel(float4* __restrict__ dst, const float4* __restrict__ src, size_t n4) {
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    for (; i + 3 * stride < n4; i += 4 * stride) {
+        const float4 a = src[i], b = src[i + stride], c = src[i + 2 * stride], d = src[i + 3 * stride];
+        dst[i] = a;
+        dst[i + stride] = b;
+        dst[i + 2 * stride] = c;
+        dst[i + 3 * stride] = d;
+    }
+    for (; i < n4; i += stride) dst[i] = src[i];
+}
+
+// Launch of copy_kernel for n floats (n a multiple of 4, both pointers
+// 16-byte aligned: whole states).
+inline cudaError_t device_copy(float* dst, const float* src, size_t n, int num_sms, cudaStream_t s) {
+    const size_t n4 = n / 4;
+    const unsigned blocks = (unsigned)std::max<size_t>(1, std::min<size_t>((n4 + 255) / 256, (size_t)num_sms * 8));
+    copy_kernel<<<blocks, 256, 0, s>>>(reinterpret_cast<float4*>(dst), reinterpret_cast<const float4*>(src), n4);
+    return cudaGetLastError();
+}
+
 // sum the per-shot gradient triples: out[i] = sum_b in[b*n + i]
 __global__ void sum_shots_kernel(const float* __restrict__ in, float* __restrict__ out, size_t n,
                                  int nb, int accumulate) {
@@ -545,6 +571,15 @@ struct Engine {
     StressMaps smaps[4];
     VelMaps vmaps[4];
     AdjMaps amap;
+    // Copy-free checkpointing (TMA mapping, binomial plan): buffer k < slots is
+    // checkpoint memory, buffer `slots` is d_fwd; per buffer the stress and
+    // velocity maps of its state, the adjoint maps reading the forward fields
+    // from it, and the forward descriptors writing to it.
+    std::vector<StressMaps> smaps_b;
+    std::vector<VelMaps> vmaps_b;
+    std::vector<AdjMaps> amaps_b;
+    DBuf d_items_b;
+    const AdjMaps* amap_cur = nullptr;  // forward fields of the adjoint pass (null: amap)
     TmaGrid tgrid{}, tgrid_a{};
     int grid_tma = 1, grid_tma_a = 1;
     bool zero_mu = false;  // some interior cell has mu == 0 (exact mode unsupported)
@@ -928,7 +963,13 @@ struct Engine {
             CUDA_TRY(cudaGetLastError());
             rb_valid = true;
         }
-        if (keep && ckpt_mode() && want_slots > 0) FWI_TRY(grow(d_snap, (size_t)want_slots * cap * state * 4));
+        if (keep && ckpt_mode() && want_slots > 0) {
+            FWI_TRY(grow(d_snap, (size_t)want_slots * cap * state * 4));
+            // the copy-free plan steps into any checkpoint buffer: cells that no
+            // pass writes (grid borders) must read as zero there too
+            if (kmap == 3 && !exact())
+                CUDA_TRY(cudaMemsetAsync(d_snap.p, 0, (size_t)want_slots * nb * state * 4, stream));
+        }
         if (exact()) {
             FWI_TRY(grow(d_nxt, (size_t)cap * state * 4));
             FWI_TRY(grow(d_exact, (size_t)cap * 9 * field * 4));
@@ -1031,6 +1072,15 @@ struct Engine {
                 x.field = (long long)field;
             }
         }
+        if (copy_free()) {
+            const int nbuf = slots + 1;
+            std::vector<ItemDesc> itb((size_t)nbuf * B);
+            for (int k = 0; k < nbuf; k++)
+                for (int b = 0; b < B; b++) fill_item(itb[(size_t)k * B + b], b, false, buf(k));
+            FWI_TRY(grow(d_items_b, itb.size() * sizeof(ItemDesc)));
+            CUDA_TRY(cudaMemcpyAsync(d_items_b.p, itb.data(), itb.size() * sizeof(ItemDesc), cudaMemcpyHostToDevice,
+                                     stream));
+        }
         CUDA_TRY(cudaMemcpyAsync(d_items_f.p, itf.data(), B * sizeof(ItemDesc), cudaMemcpyHostToDevice, stream));
         CUDA_TRY(cudaMemcpyAsync(d_items_a.p, ita.data(), B * sizeof(ItemDesc), cudaMemcpyHostToDevice, stream));
         if (rb_active)
@@ -1102,6 +1152,36 @@ struct Engine {
             FWI_TRY(make_map(&A.fsxx, f + F_SXX * field, nxt, nzt, Bcap, rb, sb, kTmaTX, kAdjTZ));
             FWI_TRY(make_map(&A.fszx, f + F_SZX * field, nxt, nzt, Bcap, rb, sb, kTmaTX, kAdjTZ));
             FWI_TRY(make_map(&A.fszz, f + F_SZZ * field, nxt, nzt, Bcap, rb, sb, kTmaTX, kAdjTZ));
+        }
+        if (copy_free()) {
+            const int nbuf = slots + 1;
+            smaps_b.assign(nbuf, smaps[0]);
+            vmaps_b.assign(nbuf, vmaps[0]);
+            amaps_b.assign(nbuf, amap);
+            const int wza = kAdjTZ + 2 * FPv;
+            for (int k = 0; k < nbuf; k++) {
+                float* st = buf(k);
+                const int nb = k < slots ? B : Bcap;  // a checkpoint buffer holds B states
+                StressMaps& S = smaps_b[k];
+                FWI_TRY(make_map(&S.vx, st + F_VX * field, nxt, nzt, nb, rb, sb, wx, wz));
+                FWI_TRY(make_map(&S.vz, st + F_VZ * field, nxt, nzt, nb, rb, sb, wx, wz));
+                FWI_TRY(make_map(&S.sxx, st + F_SXX * field, nxt, nzt, nb, rb, sb, kTmaTX, kTmaTZ));
+                FWI_TRY(make_map(&S.szx, st + F_SZX * field, nxt, nzt, nb, rb, sb, kTmaTX, kTmaTZ));
+                FWI_TRY(make_map(&S.szz, st + F_SZZ * field, nxt, nzt, nb, rb, sb, kTmaTX, kTmaTZ));
+                VelMaps& V = vmaps_b[k];
+                FWI_TRY(make_map(&V.sxx, st + F_SXX * field, nxt, nzt, nb, rb, sb, wx, kTmaTZ));
+                FWI_TRY(make_map(&V.szx, st + F_SZX * field, nxt, nzt, nb, rb, sb, wx, wz));
+                FWI_TRY(make_map(&V.szz, st + F_SZZ * field, nxt, nzt, nb, rb, sb, kTmaTX, wz));
+                FWI_TRY(make_map(&V.vx, st + F_VX * field, nxt, nzt, nb, rb, sb, kTmaTX, kTmaTZ));
+                FWI_TRY(make_map(&V.vz, st + F_VZ * field, nxt, nzt, nb, rb, sb, kTmaTX, kTmaTZ));
+                AdjMaps& A = amaps_b[k];
+                FWI_TRY(make_map(&A.fvx, st + F_VX * field, nxt, nzt, nb, rb, sb, kTmaTX, kAdjTZ));
+                FWI_TRY(make_map(&A.fvz, st + F_VZ * field, nxt, nzt, nb, rb, sb, kTmaTX, kAdjTZ));
+                FWI_TRY(make_map(&A.fsxx, st + F_SXX * field, nxt, nzt, nb, rb, sb, kTmaTX, kAdjTZ));
+                FWI_TRY(make_map(&A.fszx, st + F_SZX * field, nxt, nzt, nb, rb, sb, kTmaTX, kAdjTZ));
+                FWI_TRY(make_map(&A.fszz, st + F_SZZ * field, nxt, nzt, nb, rb, sb, kTmaTX, kAdjTZ));
+                (void)wza;
+            }
         }
         const int ntx = (nxt + kTmaTX - 1) / kTmaTX;
         const int ntz = (nzt - 2 * fpad + kTmaTZ - 1) / kTmaTZ;
@@ -1251,7 +1331,8 @@ struct Engine {
     // forward fields from the checkpointed working state (fwd_kind 1).
     void pass_stress_adj(const ItemDesc* items, int it, unsigned flags) {
         if (kmap == 3 && state_source())
-            tset.adjoint(dim3(grid_tma_a), stream, amap, items, tgrid_a, it, flags, d_err.as<int>());
+            tset.adjoint(dim3(grid_tma_a), stream, amap_cur ? *amap_cur : amap, items, tgrid_a, it, flags,
+                         d_err.as<int>());
         else
             ks.stress_a(dim3(grid_sa), stream, items, d_tiles_p, ntiles, it, flags, d_err.as<int>());
     }
@@ -1302,7 +1383,7 @@ struct Engine {
     // working forward state (d_fwd) holds state n; state n+1 is made from it
     // in d_nxt by one more forward step, then the four transposed passes run.
     int exact_step(int n) {
-        CUDA_TRY(cudaMemcpyAsync(d_nxt.p, d_fwd.p, (size_t)B * state * 4, cudaMemcpyDeviceToDevice, stream));
+        FWI_TRY(state_copy(d_nxt.as<float>(), d_fwd.as<float>()));
         const ItemDesc* itn = d_items_n.as<ItemDesc>();
         pass_stress_fwd(2, itn, n, 0u);
         pass_velocity(2, itn, n, FL_INJECT);
@@ -1317,11 +1398,54 @@ struct Engine {
         launches_now += 6;
         return FWI_OK;
     }
+    // Forward steps the backward runs for the plan (in units of fwi_dt): from
+    // the last checkpoint of the first sweep (placed by forward()) to the last
+    // unit, then every ADVANCE after that prefix, plus state n+1 of each exact
+    // reverse step.  The same count whether the plan runs directly or as a
+    // replayed graph.
+    long long plan_recompute() const {
+        size_t k = 0;
+        int last_state = 0;
+        while (k < plan.size() && plan[k].kind != Action::ADJOINT) {
+            if (plan[k].kind == Action::SAVE) last_state = plan[k].b;
+            k++;
+        }
+        long long r = (long long)(nunits() - 1) - last_state;
+        for (; k < plan.size(); k++) {
+            if (plan[k].kind == Action::ADVANCE) r += plan[k].b - plan[k].a;
+            if (plan[k].kind == Action::ADJOINT && exact()) r += 1;
+        }
+        return r;
+    }
     int state_copy(float* dst, const float* src) {
-        CUDA_TRY(cudaMemcpyAsync(dst, src, (size_t)B * state * 4, cudaMemcpyDeviceToDevice, stream));
+        CUDA_TRY(device_copy(dst, src, (size_t)B * state, num_sms, stream));
+        launches_now++;
         return FWI_OK;
     }
     float* snap(int slot) { return d_snap.as<float>() + (size_t)slot * B * state; }
+    // The binomial plan runs without state copies on the TMA mapping (the
+    // other mappings and the exact adjoint copy states in and out of slots).
+    bool copy_free() const { return kmap == 3 && ckpt_mode() && !exact() && slots > 0; }
+    float* buf(int k) { return k < slots ? snap(k) : d_fwd.as<float>(); }
+    // One recompute step (stress, velocity, source injection) from the state
+    // of step `it` in buffer x to the state of step it+1 in buffer y (x == y:
+    // in place).  Out of place, the stress pass reads velocities and
+    // stresses from x and writes the stresses to y; the velocity pass reads
+    // those stresses from y and the velocities from x; CPML memories are read
+    // from x and written to y.
+    void step_bufs(int x, int y, int it) {
+        TmaGrid gg = tgrid;
+        gg.msrc = (long long)(buf(x) - buf(y));
+        const ItemDesc* items = d_items_b.as<ItemDesc>() + (size_t)y * B;
+        tset.stress(dim3(grid_tma), stream, smaps_b[x], items, gg, it, 0u, d_err.as<int>());
+        VelMaps vm = vmaps_b[x];
+        vm.sxx = vmaps_b[y].sxx;
+        vm.szx = vmaps_b[y].szx;
+        vm.szz = vmaps_b[y].szz;
+        tset.velocity(dim3(grid_tma), stream, vm, items, gg, it, 0u, d_err.as<int>());
+        events_kernel<<<B, 256, 0, stream>>>(items, it, FL_INJECT);
+        launches_now += 3;
+    }
 
     // Run `body` directly or as a cached CUDA graph.
     template <class F>
@@ -1550,10 +1674,14 @@ struct Engine {
                 if (plan[k].kind == Action::SAVE) { last_slot = plan[k].a; last_state = plan[k].b; }
                 k++;
             }
+            const int u = unit();
+            if (copy_free()) {
+                FWI_TRY(run_plan_copy_free(k, last_slot, last_state));
+                return FWI_OK;
+            }
             // working buffer: state of the last prefix checkpoint, advanced to nft-1
             if (last_slot >= 0) FWI_TRY(state_copy(d_fwd.as<float>(), snap(last_slot)));
             else CUDA_TRY(cudaMemsetAsync(d_fwd.p, 0, (size_t)B * state * 4, stream));
-            const int u = unit();
             forward_steps(last_state * u, (nunits() - 1) * u, false, false);
             recompute += (nunits() - 1) - last_state;
             for (; k < plan.size(); k++) {
@@ -1626,7 +1754,8 @@ struct Engine {
         stats.last_backward_ms = ms;
         stats.launches = launches_now;
         stats.adjoint_steps = nt;
-        stats.recompute_steps = ckpt_mode()     ? (recompute > 0 ? recompute : plan_cost) * unit()
+        (void)recompute;  // counted while the body runs; a graph replay runs the same plan
+        stats.recompute_steps = ckpt_mode()     ? plan_recompute() * unit()
                                 : random_mode() ? (int64_t)2 * nt
                                                 : 0;
         const double k0 = out_scale(0), k1 = out_scale(1), k2 = out_scale(2);
@@ -1638,6 +1767,62 @@ struct Engine {
                 if (gr) gr[s * nf + i] = t[2 * nf + i] * k2;
             }
         bwd_done = true;
+        return FWI_OK;
+    }
+
+    // The binomial plan from action k on (the first sweep's checkpoints are in
+    // place; the last of them is `last_slot` with state `last_state`) without
+    // state copies.  The working state is tracked as the buffer that holds it:
+    // RESTORE only points at the slot's buffer, the next ADVANCE steps out of
+    // it into the working buffer, SAVE swaps the working buffer with the
+    // slot's free one (the state stays where it is), and ADJOINT reads the
+    // forward fields from whichever buffer holds them.
+    int run_plan_copy_free(size_t k, int last_slot, int last_state) {
+        const int u = unit();
+        std::vector<int> phys(slots);
+        for (int i = 0; i < slots; i++) phys[i] = i;
+        int wb = slots;  // the working buffer (d_fwd)
+        int src = last_slot >= 0 ? phys[last_slot] : wb;
+        if (last_slot < 0) CUDA_TRY(cudaMemsetAsync(buf(wb), 0, (size_t)B * state * 4, stream));
+        auto advance = [&](int t0, int t1) {
+            for (int it = t0; it < t1; it++) {
+                step_bufs(src, wb, it);
+                src = wb;
+            }
+        };
+        advance(last_state * u, (nunits() - 1) * u);
+        for (; k < plan.size(); k++) {
+            const Action& a = plan[k];
+            switch (a.kind) {
+                case Action::ADVANCE:
+                    advance(a.a * u, a.b * u);
+                    break;
+                case Action::SAVE:
+                    if (src == wb) {
+                        std::swap(phys[a.a], wb);
+                        src = phys[a.a];
+                    } else {
+                        FWI_TRY(state_copy(buf(phys[a.a]), buf(src)));
+                        src = phys[a.a];
+                    }
+                    break;
+                case Action::RESTORE:
+                    if (a.a < 0) {
+                        CUDA_TRY(cudaMemsetAsync(buf(wb), 0, (size_t)B * state * 4, stream));
+                        src = wb;
+                    } else {
+                        src = phys[a.a];
+                    }
+                    break;
+                case Action::ADJOINT: {
+                    const int t0 = a.a * fwi_dt, t1 = std::min(nt, (a.a + 1) * fwi_dt);
+                    amap_cur = &amaps_b[src];
+                    adjoint_steps(t0, t1);
+                    amap_cur = nullptr;
+                    break;
+                }
+            }
+        }
         return FWI_OK;
     }
 

@@ -398,7 +398,7 @@ struct MultiEngine {
             step(false, it, 0u, FL_INJECT | (record ? (FL_RECORD | FL_WE) : 0u));
     }
     int state_copy(float* dst, const float* src) {
-        CUDA_TRY(cudaMemcpyAsync(dst, src, total_state * 4, cudaMemcpyDeviceToDevice, stream));
+        CUDA_TRY(device_copy(dst, src, total_state, num_sms, stream));
         return FWI_OK;
     }
     float* snap(int s) { return d_snap.as<float>() + (size_t)s * total_state; }

@@ -84,6 +84,10 @@ struct TmaGrid {
     int nb, ntz, ntiles, pad;
     int cxl, cxh, czl, czh;
     int gxl, gxh, gzl, gzh;
+    // forward passes: offset (floats) from the written state to the state the
+    // CPML memories are read from (0 in place; a step out of a checkpoint
+    // buffer into the working buffer reads them from the checkpoint)
+    long long msrc;
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -323,7 +327,8 @@ __device__ __forceinline__ void stress_issue(const StressMaps& m, const ItemDesc
 
 template <int FP, bool INTERIOR>
 __device__ __forceinline__ void stress_rows(const ItemDesc& D, const float* st, int x0, int z0, int it,
-                                            unsigned flags, const float2 (&hx)[FP], const float2 (&hz)[FP]) {
+                                            unsigned flags, const float2 (&hx)[FP], const float2 (&hz)[FP],
+                                            long long msrc) {
     using G = TmaGeom<FP>;
     constexpr int R = kPairRows;
     constexpr int W = R + 2 * FP - 1;
@@ -369,14 +374,14 @@ __device__ __forceinline__ void stress_rows(const ItemDesc& D, const float* st, 
             for (int l = 0; l < 2; l++) {
                 mx1[rr][l] = mx2[rr][l] = 0.f;
                 if (pc.px[l] >= 0 && iz < nzt - FP) {
-                    mx1[rr][l] = mvx_x[(size_t)iz * tp + pc.px[l]];
-                    mx2[rr][l] = mvz_x[(size_t)iz * tp + pc.px[l]];
+                    mx1[rr][l] = (mvx_x + msrc)[(size_t)iz * tp + pc.px[l]];
+                    mx2[rr][l] = (mvz_x + msrc)[(size_t)iz * tp + pc.px[l]];
                 }
             }
             pzr[rr] = strip_z<FP>(D, iz, true);
             if (pzr[rr] >= 0) {
-                mz1[rr] = ld2(mvz_z + (size_t)pzr[rr] * P + ix);
-                mz2[rr] = ld2(mvx_z + (size_t)pzr[rr] * P + ix);
+                mz1[rr] = ld2(mvz_z + msrc + (size_t)pzr[rr] * P + ix);
+                mz2[rr] = ld2(mvx_z + msrc + (size_t)pzr[rr] * P + ix);
             }
         }
         // sampled window columns (forward storage for the gradient)
@@ -475,8 +480,8 @@ template <int FP>
 __device__ __forceinline__ void stress_compute(const ItemDesc& D, const TmaGrid& g, const float* st, int x0, int z0,
                                                int it, unsigned flags, const float2 (&hx)[FP],
                                                const float2 (&hz)[FP]) {
-    if (interior_warp(g, x0, z0, flags)) stress_rows<FP, true>(D, st, x0, z0, it, flags, hx, hz);
-    else stress_rows<FP, false>(D, st, x0, z0, it, flags, hx, hz);
+    if (interior_warp(g, x0, z0, flags)) stress_rows<FP, true>(D, st, x0, z0, it, flags, hx, hz, g.msrc);
+    else stress_rows<FP, false>(D, st, x0, z0, it, flags, hx, hz, g.msrc);
 }
 
 // ---------------------------------------------------------------------------
@@ -503,7 +508,7 @@ __device__ __forceinline__ void velocity_issue(const VelMaps& m, const ItemDesc*
 
 template <int FP, bool INTERIOR>
 __device__ __forceinline__ void velocity_rows(const ItemDesc& D, const float* st, int x0, int z0, unsigned flags,
-                                              const float2 (&hx)[FP], const float2 (&hz)[FP]) {
+                                              const float2 (&hx)[FP], const float2 (&hz)[FP], long long msrc) {
     using G = TmaGeom<FP>;
     constexpr int R = kPairRows;
     constexpr int W = R + 2 * FP - 1;
@@ -547,14 +552,14 @@ __device__ __forceinline__ void velocity_rows(const ItemDesc& D, const float* st
             for (int l = 0; l < 2; l++) {
                 mx1[rr][l] = mx2[rr][l] = 0.f;
                 if (pc.px[l] >= 0 && iz < nzt - FP) {
-                    mx1[rr][l] = msxx_x[(size_t)iz * tp + pc.px[l]];
-                    mx2[rr][l] = mszx_x[(size_t)iz * tp + pc.px[l]];
+                    mx1[rr][l] = (msxx_x + msrc)[(size_t)iz * tp + pc.px[l]];
+                    mx2[rr][l] = (mszx_x + msrc)[(size_t)iz * tp + pc.px[l]];
                 }
             }
             pzr[rr] = strip_z<FP>(D, iz, false);
             if (pzr[rr] >= 0) {
-                mz1[rr] = ld2(mszz_z + (size_t)pzr[rr] * P + ix);
-                mz2[rr] = ld2(mszx_z + (size_t)pzr[rr] * P + ix);
+                mz1[rr] = ld2(mszz_z + msrc + (size_t)pzr[rr] * P + ix);
+                mz2[rr] = ld2(mszx_z + msrc + (size_t)pzr[rr] * P + ix);
             }
         }
     }
@@ -615,8 +620,8 @@ template <int FP>
 __device__ __forceinline__ void velocity_compute(const ItemDesc& D, const TmaGrid& g, const float* st, int x0,
                                                  int z0, unsigned flags, const float2 (&hx)[FP],
                                                  const float2 (&hz)[FP]) {
-    if (interior_warp(g, x0, z0, flags)) velocity_rows<FP, true>(D, st, x0, z0, flags, hx, hz);
-    else velocity_rows<FP, false>(D, st, x0, z0, flags, hx, hz);
+    if (interior_warp(g, x0, z0, flags)) velocity_rows<FP, true>(D, st, x0, z0, flags, hx, hz, g.msrc);
+    else velocity_rows<FP, false>(D, st, x0, z0, flags, hx, hz, g.msrc);
 }
 
 // Stencil weights of a launch (every slot of a launch has the same grid),

@@ -22,7 +22,7 @@ pytestmark = pytest.mark.gpu
 
 SEIS_TOL = 1e-5
 GRAD_TOL = 1e-4
-TX, TZ = 128, 16  # TMA tile of the forward passes; a warp: 64 columns x 2 rows
+TX, TZ, WR = 128, 16, 2  # TMA tile of the forward passes; a warp: 64 columns x WR rows
 
 
 def _warps(p):
@@ -40,8 +40,8 @@ def _warps(p):
     for x0 in range(0, p.nxt, TX):
         for z0 in range(fp, p.nzt - fp, TZ):
             for wx in (x0, x0 + 64):
-                for wz in range(z0, z0 + TZ, 2):
-                    nin += wx >= cxl and wx + 63 <= cxh and wz >= czl and wz + 1 <= czh
+                for wz in range(z0, z0 + TZ, WR):
+                    nin += wx >= cxl and wx + 63 <= cxh and wz >= czl and wz + WR - 1 <= czh
                     ntot += 1
     return nin, ntot
 
@@ -104,3 +104,28 @@ def test_interior_tiles_random_boundary():
     assert mis[0] == pytest.approx(J, rel=1e-4)
     for i in range(3):
         assert rel_l2(g[i][0], g_o[i]) <= 1e-3, i
+
+
+@pytest.mark.parametrize("strategy", ["binomial", "random"])
+def test_many_tiles_per_cta_batch_equals_single_shots(strategy):
+    """16 shots of a 600x200 grid: ~7 forward tiles per CTA, so every stage of
+    the TMA pipelines is refilled several times; each shot of the batch must be
+    bitwise the shot computed alone (one tile per CTA at most)."""
+    p = P.small(fdorder=8, nx=600, nz=200, nt=120, npml=8, nshots=16, nrec=6, perturb=0.04)
+    fp = p.fdorder // 2
+    tiles = -(-p.nxt // TX) * -(-(p.nzt - 2 * fp) // TZ) * 16
+    assert tiles >= 7 * 152
+    obs = np.zeros((p.nrec, p.nt))
+    shots = list(range(16))
+    with Engine(p) as eng:
+        eng.set_strategy(strategy, **({"snapshots": 5} if strategy == "binomial" else {}))
+        rec_b, mis_b = eng.forward(shots, obs, keep=True)  # one batch: all 16 shots per launch
+        g_b = eng.backward()
+        for s in (0, 7, 15):
+            rec_s, mis_s = eng.forward([s], obs, keep=True)
+            g_s = eng.backward()
+            rows = O.shot_rows(p, s)
+            assert np.array_equal(rec_s[rows], rec_b[rows]), s
+            assert mis_s[0] == mis_b[s]
+            for i in range(3):
+                assert np.array_equal(g_s[i][0], g_b[i][s]), (s, i)

@@ -5,6 +5,7 @@ reference's outputs (golden fixtures, fdorder 2) and the FP64 CPU oracle
 import numpy as np
 import pytest
 
+import _plan
 from _fixtures import load
 from conftest import rel_l2
 from cuda_fwi_gb300 import _capi
@@ -184,7 +185,11 @@ def test_binomial_checkpointing_equals_full_storage(fwi, snaps, bx):
             assert np.array_equal(g_f[i], g_c[i]), i
         else:
             assert rel_l2(g_c[i], g_f[i]) <= 3e-5, i
-    assert st["recompute_steps"] > 0
+    if snaps:
+        # forward steps the backward actually runs (the first sweep placed
+        # its checkpoints), in time steps
+        want = _plan.recompute_after_first_sweep(p.nft, min(snaps, p.nft - 1)) * p.fwi_dt
+        assert st["recompute_steps"] == want > 0
 
 
 def test_graphs_and_direct_launches_agree():
