@@ -312,6 +312,8 @@ def main():
     sub = int(st["batch"])
     value = world * B * args.steps / dev_s
     gcell = world * B * cells * steps_per_batch * args.steps / dev_s / 1e9
+    # "useful" rate: 2 nt propagation steps per shot-gradient (no recompute counted)
+    gcell_useful = world * B * cells * 2 * syn.nt * args.steps / dev_s / 1e9
 
     # ---- roofline: live per-kernel timing on one full sub-batch ----
     eng.forward(shots[:sub], obs, keep=True, want_rec=False)  # lays out a batch of `sub` shots
@@ -439,6 +441,7 @@ def main():
                              "checkpoints, 192 MB observed data)",
                        "parallelism": f"replicas x{world}, shots batched in one launch per time step"},
             "gcell_upd_s": gcell,
+            "gcell_upd_s_useful": gcell_useful,
             "time_steps_per_shot_gradient": steps_per_batch,
             "e2e": {"value": world * B * args.steps / e2e_s, "unit": "shot-gradients/s",
                     "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
