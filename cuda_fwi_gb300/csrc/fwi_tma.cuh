@@ -846,9 +846,18 @@ struct GradAhead {
     bool valid;
 };
 
-template <int FP, bool INTERIOR>
-__device__ __forceinline__ void adjoint_rows(const ItemDesc& D, const float* st, int x0, int z0, bool grad_step,
+// Reciprocal with the approximate instruction (relative error ~1 ulp; the
+// gradient's tolerance is 1e-4 relative L2).
+__device__ __forceinline__ float rcp_approx(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+template <int FP, bool INTERIOR, bool GRAD>
+__device__ __forceinline__ void adjoint_rows(const ItemDesc& D, const float* st, int x0, int z0,
                                              const float2 (&hx)[FP], const float2 (&hz)[FP], const GradAhead& ga) {
+    constexpr bool grad_step = GRAD;
     using G = AdjGeom<FP>;
     const int cp = (threadIdx.x & (kTmaTX / 2 - 1)) * 2;
     const int r = threadIdx.x / (kTmaTX / 2);  // tile row
@@ -867,7 +876,7 @@ __device__ __forceinline__ void adjoint_rows(const ItemDesc& D, const float* st,
     float* __restrict__ glam = D.glam;
     float* __restrict__ gmu = D.gmu;
     float* __restrict__ grho = D.grho;
-    if (grad_step) {
+    if constexpr (grad_step) {
         if constexpr (INTERIOR) {
             gi[0] = (iz - D.wz1) * D.nfx + (ix - D.wx1);
             gi[1] = gi[0] + 1;
@@ -960,9 +969,9 @@ __device__ __forceinline__ void adjoint_rows(const ItemDesc& D, const float* st,
     const float2 dt2 = bc2(D.dt);
     const float2 ux = fma2(dt2, cvx, ld2(cen + 6 * G::CEN + ci));
     const float2 uz = fma2(dt2, cvz, ld2(cen + 7 * G::CEN + ci));
-    if (gi[0] >= 0 || gi[1] >= 0) {
-        // the stored velocities are v/dt; correctly rounded reciprocals in place
-        // of the divisions (rounding within the gradient tolerance)
+    if (GRAD && (INTERIOR || gi[0] >= 0 || gi[1] >= 0)) {
+        // the stored velocities are v/dt; reciprocals in place of the divisions
+        // (rounding within the gradient tolerance)
         const float2 idt = bc2(D.inv_dt);
         const float2 fvx = mul2(ld2(cen + 8 * G::CEN + ci), idt), fvz = mul2(ld2(cen + 9 * G::CEN + ci), idt);
         const float2 fsxx = ld2(cen + 10 * G::CEN + ci), fszx = ld2(cen + 11 * G::CEN + ci);
@@ -970,8 +979,8 @@ __device__ __forceinline__ void adjoint_rows(const ItemDesc& D, const float* st,
         const float2 lpm = mul2(fma2(bc2(0.5f), M2, L), idt);
         const float2 mu = mul2(mul2(bc2(0.5f), M2), idt);
         const float2 lpm2 = mul2(lpm, lpm), mu2 = mul2(mu, mu);
-        const float2 ilpm2 = make_float2(0.25f * __frcp_rn(lpm2.x), 0.25f * __frcp_rn(lpm2.y));
-        const float2 imu2 = make_float2(__frcp_rn(mu2.x), __frcp_rn(mu2.y));
+        const float2 ilpm2 = make_float2(0.25f * rcp_approx(lpm2.x), 0.25f * rcp_approx(lpm2.y));
+        const float2 imu2 = make_float2(rcp_approx(mu2.x), rcp_approx(mu2.y));
         const float2 s1 = mul2(mul2(add2(fsxx, fszz), add2(sxx, szz)), ilpm2);
         const float2 s2 = mul2(mul2(sub2(fsxx, fszz), sub2(sxx, szz)), imu2);
         const float2 s3 = mul2(mul2(fszx, szx), imu2);
@@ -982,7 +991,7 @@ __device__ __forceinline__ void adjoint_rows(const ItemDesc& D, const float* st,
         const float2 nr = fma2(make_float2(-D.gscale, -D.gscale), s4, make_float2(g2[0], g2[1]));
 #pragma unroll
         for (int l = 0; l < 2; l++) {
-            if (gi[l] >= 0) {
+            if (INTERIOR || gi[l] >= 0) {
                 glam[gi[l]] = lane(nl, l);
                 gmu[gi[l]] = lane(nm, l);
                 grho[gi[l]] = lane(nr, l);
@@ -1039,8 +1048,14 @@ __global__ void __launch_bounds__(kTmaThreads, 1)
         },
         [&](int4 c, int4 n, const float* st) {
             const ItemDesc& D = *reinterpret_cast<const ItemDesc*>(st + G::DESC);
-            if (interior_warp_adj(g, c.y, c.z, grad)) adjoint_rows<FP, true>(D, st, c.y, c.z, grad, hx, hz, ga);
-            else adjoint_rows<FP, false>(D, st, c.y, c.z, grad, hx, hz, ga);
+            const bool in = interior_warp_adj(g, c.y, c.z, grad);
+            if (grad) {
+                if (in) adjoint_rows<FP, true, true>(D, st, c.y, c.z, hx, hz, ga);
+                else adjoint_rows<FP, false, true>(D, st, c.y, c.z, hx, hz, ga);
+            } else {
+                if (in) adjoint_rows<FP, true, false>(D, st, c.y, c.z, hx, hz, ga);
+                else adjoint_rows<FP, false, false>(D, st, c.y, c.z, hx, hz, ga);
+            }
             ga.valid = false;
             if (grad && n.x >= 0 && interior_warp_adj(g, n.y, n.z, true)) {
                 const ItemDesc* In = items + n.x;
