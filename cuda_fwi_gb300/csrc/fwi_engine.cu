@@ -1829,13 +1829,23 @@ struct Engine {
     // ---- gradient over many shots in sub-batches --------------------------------
     int batch_override = 0;
 
-    // Shots per launch: enough cells per launch to fill the GPU with a few
-    // waves of blocks (about 8 M cells; measured on the 1068x568 grid, order
-    // 8: 3.5 shot-gradients/s at 4 shots per launch, 3.8 at 8-16, 3.6 at 64).
+    // Shots per launch: about 20 M cells per launch (measured on the 1068x568
+    // grid, order 8, TMA mapping, 64 shots: 7.98 shot-gradients/s at 14 shots
+    // per launch, 8.11 at 16, 8.25 at 32, 8.20 at 64), the shots split evenly
+    // over the sub-batches, and a batch (its checkpoints or storage included)
+    // within 80 % of the device memory or the engine's budget.
     int auto_batch(int n) const {
         const double cells = (double)(nxt - 2 * fpad) * (double)(nzt - 2 * fpad);
-        const int b = (int)std::ceil(8.0e6 / std::max(1.0, cells));
-        return std::max(1, std::min(n, b));
+        int bmax = std::max(1, std::min(n, (int)std::ceil(2.0e7 / std::max(1.0, cells))));
+        size_t bud = budget;
+        if (bud == 0) {
+            size_t fr = 0, tot = 0;
+            if (cudaMemGetInfo(&fr, &tot) == cudaSuccess) bud = (size_t)(0.8 * (double)(fr + allocated_bytes()));
+        }
+        const int sl = snapshots_req > 0 ? std::min(snapshots_req, std::max(1, nunits() - 1)) : 0;
+        while (bud > 0 && bmax > 1 && batch_bytes(bmax, sl, strategy) + fixed_bytes() > bud) bmax--;
+        const int nsub = (n + bmax - 1) / bmax;
+        return std::max(1, (n + nsub - 1) / nsub);
     }
 
     int gradient(int n, const int* ids, const double* obs, double* misfit, double* gl, double* gm,
