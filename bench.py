@@ -152,7 +152,9 @@ def cpu_baseline(syn, args, nproc=None):
                        f"(forward with full storage + adjoint + gradient, FP64 order-8 restatement of the "
                        f"reference CPU path) over {r['nt_sample']} of {syn.nt} time steps on the full "
                        f"1068x568 grid, time scaled by nt/{r['nt_sample']}; {r['sample_s']:.1f} s wall"),
-            "gcell_upd_s": r["gcell_per_s"]}
+            "gcell_upd_s": r["gcell_per_s"],
+            # one process = one core (all cores busy at the same time)
+            "per_core_value": 1.0 / (r["per_process_s"] * syn.nt / r["nt_sample"])}
 
 
 def run_reference(args, rank):
@@ -398,7 +400,7 @@ def main():
         mu.close()
         # the batch against the one-model engine running the same kernels (the
         # order group's tuned mapping): only the batching differs
-        bx = {"vectorised cells": 64, "scalar cells": 32, "z-march": 128}
+        bx = {"vectorised cells": 64, "scalar cells": 32, "z-march": 128, "TMA-staged tiles": 256}
         errs = []
         for k in range(min(args.uneven_check, len(syns))):
             t = next(t_ for t_ in tuning if t_["half_order"] == syns[k].fpad)
