@@ -86,8 +86,16 @@ __global__ void residual_kernel(const float* __restrict__ syn, const float* __re
 // cell are added in event order by one thread (events are sorted by column,
 // row, injections first), then the receivers read vz
 // (forward_kernel_PSV_GPU.cu:1033-1063 order).
+__device__ __forceinline__ void slot_events(const ItemDesc& D, int it, unsigned flags);
 __global__ void events_kernel(const ItemDesc* __restrict__ items, int it, unsigned flags) {
-    const ItemDesc& D = items[blockIdx.x];
+    slot_events(items[blockIdx.x], it, flags);
+}
+// the same for the models listed in ids (one block each)
+__global__ void events_list_kernel(const ItemDesc* __restrict__ items, const int* __restrict__ ids, int it,
+                                   unsigned flags) {
+    slot_events(items[ids[blockIdx.x]], it, flags);
+}
+__device__ __forceinline__ void slot_events(const ItemDesc& D, int it, unsigned flags) {
     const int e0 = D.ev_col[0], e1 = D.ev_col[D.nxt];
     const int nt = D.nt, P = D.pitch;
     if (flags & FL_INJECT)
@@ -379,6 +387,76 @@ static TmaSet tma_for(int fp) {
         case 4: return tma_set<4>();
         case 5: return tma_set<5>();
         default: return tma_set<6>();
+    }
+}
+
+// Forward steps a backward runs for a binomial plan over n units: from the
+// last checkpoint of the first sweep (placed while the forward records) to
+// the last unit, then every ADVANCE after that prefix, plus state n+1 of each
+// reverse step of the exact adjoint.  The same count whether the plan runs
+// directly or as a replayed graph.
+static long long plan_recompute_steps(const std::vector<Action>& plan, int n, bool exact_steps) {
+    size_t k = 0;
+    int last_state = 0;
+    while (k < plan.size() && plan[k].kind != Action::ADJOINT) {
+        if (plan[k].kind == Action::SAVE) last_state = plan[k].b;
+        k++;
+    }
+    long long r = (long long)(n - 1) - last_state;
+    for (; k < plan.size(); k++) {
+        if (plan[k].kind == Action::ADVANCE) r += plan[k].b - plan[k].a;
+        if (plan[k].kind == Action::ADJOINT && exact_steps) r += 1;
+    }
+    return r;
+}
+
+// TMA-staged passes over a work-list of tiles of several models (the
+// multi-model engine; maps per model in device memory).
+using TmaMultiFn = void (*)(dim3, cudaStream_t, const MultiMaps*, const ItemDesc*, const Tile*, int, int, unsigned,
+                            int, int*);
+struct TmaMultiSet {
+    TmaMultiFn stress, velocity, adjoint;  // velocity: int argument = adjoint state
+    cudaError_t (*prepare)();
+};
+template <int FP>
+static void tm_stress(dim3 g, cudaStream_t s, const MultiMaps* m, const ItemDesc* it, const Tile* t, int nt, int step,
+                      unsigned flags, int, int* err) {
+    stress_tma_multi_kernel<FP><<<g, kTmaThreads, stress_tma_smem<FP>(), s>>>(m, it, t, nt, step, flags, err);
+}
+template <int FP>
+static void tm_velocity(dim3 g, cudaStream_t s, const MultiMaps* m, const ItemDesc* it, const Tile* t, int nt,
+                        int step, unsigned flags, int adj, int* err) {
+    velocity_tma_multi_kernel<FP><<<g, kTmaThreads, velocity_tma_smem<FP>(), s>>>(m, it, t, nt, step, flags, adj,
+                                                                                     err);
+}
+template <int FP>
+static void tm_adjoint(dim3 g, cudaStream_t s, const MultiMaps* m, const ItemDesc* it, const Tile* t, int nt,
+                       int step, unsigned flags, int, int* err) {
+    adjoint_tma_multi_kernel<FP><<<g, kTmaThreads, adjoint_tma_smem<FP>(), s>>>(m, it, t, nt, step, flags, err);
+}
+template <int FP>
+static cudaError_t tm_prepare() {
+    cudaError_t e = cudaFuncSetAttribute(stress_tma_multi_kernel<FP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)stress_tma_smem<FP>());
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(adjoint_tma_multi_kernel<FP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)adjoint_tma_smem<FP>());
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(velocity_tma_multi_kernel<FP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)velocity_tma_smem<FP>());
+}
+template <int FP>
+static TmaMultiSet tma_multi_set() {
+    return {tm_stress<FP>, tm_velocity<FP>, tm_adjoint<FP>, tm_prepare<FP>};
+}
+static TmaMultiSet tma_multi_for(int fp) {
+    switch (fp) {
+        case 1: return tma_multi_set<1>();
+        case 2: return tma_multi_set<2>();
+        case 3: return tma_multi_set<3>();
+        case 4: return tma_multi_set<4>();
+        case 5: return tma_multi_set<5>();
+        default: return tma_multi_set<6>();
     }
 }
 
@@ -1403,20 +1481,7 @@ struct Engine {
     // unit, then every ADVANCE after that prefix, plus state n+1 of each exact
     // reverse step.  The same count whether the plan runs directly or as a
     // replayed graph.
-    long long plan_recompute() const {
-        size_t k = 0;
-        int last_state = 0;
-        while (k < plan.size() && plan[k].kind != Action::ADJOINT) {
-            if (plan[k].kind == Action::SAVE) last_state = plan[k].b;
-            k++;
-        }
-        long long r = (long long)(nunits() - 1) - last_state;
-        for (; k < plan.size(); k++) {
-            if (plan[k].kind == Action::ADVANCE) r += plan[k].b - plan[k].a;
-            if (plan[k].kind == Action::ADJOINT && exact()) r += 1;
-        }
-        return r;
-    }
+    long long plan_recompute() const { return plan_recompute_steps(plan, nunits(), exact()); }
     int state_copy(float* dst, const float* src) {
         CUDA_TRY(device_copy(dst, src, (size_t)B * state, num_sms, stream));
         launches_now++;
@@ -2247,9 +2312,9 @@ int fwi_psv_multi_tuning(fwi_psv_multi* h, int group, int info[7], double ms[2])
     const auto& g = *h->m.groups[group];
     info[0] = g.fp;
     info[1] = (int)g.members.size();
-    info[2] = g.kf.map;
+    info[2] = g.tune.fmap == 3 ? 3 : g.kf.map;  // the kernel set's map (a half order may not have map 2)
     info[3] = g.tune.ftz;
-    info[4] = g.ka.map;
+    info[4] = g.tune.amap == 3 ? 3 : g.ka.map;
     info[5] = g.tune.atz;
     info[6] = g.tune.cached ? 1 : 0;
     ms[0] = g.tune.fms;

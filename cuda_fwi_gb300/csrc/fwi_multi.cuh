@@ -58,11 +58,15 @@ struct MultiEngine {
     size_t total_rec = 0, total_src = 0;
     DBuf d_fwd, d_adj, d_ws, d_wr, d_ux, d_uz, d_grad, d_mat, d_cpml, d_srcsig, d_rec, d_resid, d_obs;
     DBuf d_rowmis, d_blow, d_snap, d_items_f, d_items_a, d_evcol, d_ev, d_evx, d_err, d_rows;
+    DBuf d_mmaps, d_gids;   // TMA maps per model; member lists of the groups (events)
+    bool mmaps_built = false;
     struct Group {
         int fp = 0;
         std::vector<int> members;  // item indices, nt descending
         TuneChoice tune;
         KernelSet kf{}, ka{};
+        TmaMultiSet tm{};
+        int gid_off = 0;  // this group's member list in d_gids
         DBuf tiles_f, tiles_a;
         std::vector<int> cum_f, cum_a;  // tiles of the first k members
         int occ_f = 1, occ_v = 1, occ_a = 1;
@@ -288,7 +292,73 @@ struct MultiEngine {
         for (auto& g : groups)
             std::stable_sort(g->members.begin(), g->members.end(),
                              [&](int u, int v) { return items[u].nt > items[v].nt; });
+        std::vector<int> gids;
+        for (auto& g : groups) {
+            g->gid_off = (int)gids.size();
+            gids.insert(gids.end(), g->members.begin(), g->members.end());
+        }
+        FWI_TRY(d_gids.ensure(gids.size() * 4));
+        CUDA_TRY(cudaMemcpy(d_gids.p, gids.data(), gids.size() * 4, cudaMemcpyHostToDevice));
         for (auto& g : groups) FWI_TRY(apply_choice(*g, g->tune));
+        return FWI_OK;
+    }
+
+    // Tensor maps of every model's states for the TMA-staged passes (one slot
+    // per map; addresses are fixed for the engine's lifetime).
+    int build_mmaps() {
+        if (mmaps_built) return FWI_OK;
+        std::vector<MultiMaps> mm(n);
+        for (int b = 0; b < n; b++) {
+            const MultiItem& I = items[b];
+            const int FPv = I.fpad, hx = (FPv + 3) / 4 * 4;
+            const int wx = kTmaTX + 2 * hx, wz = kTmaTZ + 2 * FPv, wza = kAdjTZ + 2 * FPv;
+            const size_t rb = (size_t)I.pitch * 4, sb = I.state * 4, fb = I.field * 4, f = I.field;
+            const float* mat = d_mat.as<float>() + I.off_mat;
+            float* sf = d_fwd.as<float>() + I.off_state;
+            float* sa = d_adj.as<float>() + I.off_state;
+            const int X = I.nxt, Z = I.nzt;
+            MultiMaps& M = mm[b];
+            FWI_TRY(make_map(&M.sf.vx, sf + F_VX * f, X, Z, 1, rb, sb, wx, wz));
+            FWI_TRY(make_map(&M.sf.vz, sf + F_VZ * f, X, Z, 1, rb, sb, wx, wz));
+            FWI_TRY(make_map(&M.sf.L, mat, X, Z, 0, rb, 0, kTmaTX, kTmaTZ));
+            FWI_TRY(make_map(&M.sf.M2, mat + f, X, Z, 0, rb, 0, kTmaTX, kTmaTZ));
+            FWI_TRY(make_map(&M.sf.MZ, mat + 2 * f, X, Z, 0, rb, 0, kTmaTX, kTmaTZ));
+            FWI_TRY(make_map(&M.sf.sxx, sf + F_SXX * f, X, Z, 1, rb, sb, kTmaTX, kTmaTZ));
+            FWI_TRY(make_map(&M.sf.szx, sf + F_SZX * f, X, Z, 1, rb, sb, kTmaTX, kTmaTZ));
+            FWI_TRY(make_map(&M.sf.szz, sf + F_SZZ * f, X, Z, 1, rb, sb, kTmaTX, kTmaTZ));
+            for (int a = 0; a < 2; a++) {
+                VelMaps& V = a ? M.va : M.vf;
+                float* st = a ? sa : sf;
+                float* we = (a ? d_wr.as<float>() : d_ws.as<float>()) + I.off_field;
+                FWI_TRY(make_map(&V.sxx, st + F_SXX * f, X, Z, 1, rb, sb, wx, kTmaTZ));
+                FWI_TRY(make_map(&V.szx, st + F_SZX * f, X, Z, 1, rb, sb, wx, wz));
+                FWI_TRY(make_map(&V.szz, st + F_SZZ * f, X, Z, 1, rb, sb, kTmaTX, wz));
+                FWI_TRY(make_map(&V.BX, mat + 3 * f, X, Z, 0, rb, 0, kTmaTX, kTmaTZ));
+                FWI_TRY(make_map(&V.BZ, mat + 4 * f, X, Z, 0, rb, 0, kTmaTX, kTmaTZ));
+                FWI_TRY(make_map(&V.vx, st + F_VX * f, X, Z, 1, rb, sb, kTmaTX, kTmaTZ));
+                FWI_TRY(make_map(&V.vz, st + F_VZ * f, X, Z, 1, rb, sb, kTmaTX, kTmaTZ));
+                FWI_TRY(make_map(&V.We, we, X, Z, 1, rb, fb, kTmaTX, kTmaTZ));
+            }
+            AdjMaps& A = M.a;
+            FWI_TRY(make_map(&A.vx, sa + F_VX * f, X, Z, 1, rb, sb, wx, wza));
+            FWI_TRY(make_map(&A.vz, sa + F_VZ * f, X, Z, 1, rb, sb, wx, wza));
+            FWI_TRY(make_map(&A.L, mat, X, Z, 0, rb, 0, kTmaTX, kAdjTZ));
+            FWI_TRY(make_map(&A.M2, mat + f, X, Z, 0, rb, 0, kTmaTX, kAdjTZ));
+            FWI_TRY(make_map(&A.MZ, mat + 2 * f, X, Z, 0, rb, 0, kTmaTX, kAdjTZ));
+            FWI_TRY(make_map(&A.sxx, sa + F_SXX * f, X, Z, 1, rb, sb, kTmaTX, kAdjTZ));
+            FWI_TRY(make_map(&A.szx, sa + F_SZX * f, X, Z, 1, rb, sb, kTmaTX, kAdjTZ));
+            FWI_TRY(make_map(&A.szz, sa + F_SZZ * f, X, Z, 1, rb, sb, kTmaTX, kAdjTZ));
+            FWI_TRY(make_map(&A.ux, d_ux.as<float>() + I.off_field, X, Z, 1, rb, fb, kTmaTX, kAdjTZ));
+            FWI_TRY(make_map(&A.uz, d_uz.as<float>() + I.off_field, X, Z, 1, rb, fb, kTmaTX, kAdjTZ));
+            FWI_TRY(make_map(&A.fvx, sf + F_VX * f, X, Z, 1, rb, sb, kTmaTX, kAdjTZ));
+            FWI_TRY(make_map(&A.fvz, sf + F_VZ * f, X, Z, 1, rb, sb, kTmaTX, kAdjTZ));
+            FWI_TRY(make_map(&A.fsxx, sf + F_SXX * f, X, Z, 1, rb, sb, kTmaTX, kAdjTZ));
+            FWI_TRY(make_map(&A.fszx, sf + F_SZX * f, X, Z, 1, rb, sb, kTmaTX, kAdjTZ));
+            FWI_TRY(make_map(&A.fszz, sf + F_SZZ * f, X, Z, 1, rb, sb, kTmaTX, kAdjTZ));
+        }
+        FWI_TRY(d_mmaps.ensure(mm.size() * sizeof(MultiMaps)));
+        CUDA_TRY(cudaMemcpy(d_mmaps.p, mm.data(), mm.size() * sizeof(MultiMaps), cudaMemcpyHostToDevice));
+        mmaps_built = true;
         return FWI_OK;
     }
 
@@ -337,9 +407,10 @@ struct MultiEngine {
         }
     }
 
-    // tiles of a group for a mapping (map 0: tz rows per tile; cell maps: their own height)
-    int plan_group(Group& g, int map, int tz, DBuf& buf, std::vector<int>& cum) {
-        const int rows = map == 0 ? tz : MapDims<2>::rows;
+    // tiles of a group for a mapping (map 0: tz rows per tile; cell maps: their
+    // own height; 3: the TMA tiles, 128 x 16 forward and 128 x 8 adjoint)
+    int plan_group(Group& g, int map, int tz, DBuf& buf, std::vector<int>& cum, bool adj) {
+        const int rows = map == 0 ? tz : map == 3 ? (adj ? kAdjTZ : kTmaTZ) : MapDims<2>::rows;
         std::vector<Tile> t;
         cum.assign(1, 0);
         for (int b : g.members) {
@@ -357,13 +428,18 @@ struct MultiEngine {
 
     int apply_choice(Group& g, const TuneChoice& c) {
         g.tune = c;
-        g.kf = kernels_for(g.fp, c.fmap);
-        g.ka = kernels_for(g.fp, c.amap);
+        g.kf = kernels_for(g.fp, c.fmap == 3 ? 1 : c.fmap);
+        g.ka = kernels_for(g.fp, c.amap == 3 ? 1 : c.amap);
         g.occ_f = std::max(1, g.kf.occ_f());
         g.occ_v = std::max(1, g.kf.occ_v());
         g.occ_a = std::max(1, g.ka.occ_a());
-        FWI_TRY(plan_group(g, g.kf.map, c.ftz, g.tiles_f, g.cum_f));
-        FWI_TRY(plan_group(g, g.ka.map, c.atz, g.tiles_a, g.cum_a));
+        if (c.fmap == 3 || c.amap == 3) {
+            FWI_TRY(build_mmaps());
+            g.tm = tma_multi_for(g.fp);
+            CUDA_TRY(g.tm.prepare());
+        }
+        FWI_TRY(plan_group(g, c.fmap == 3 ? 3 : g.kf.map, c.ftz, g.tiles_f, g.cum_f, false));
+        FWI_TRY(plan_group(g, c.amap == 3 ? 3 : g.ka.map, c.atz, g.tiles_a, g.cum_a, true));
         drop_graphs();
         return FWI_OK;
     }
@@ -378,18 +454,37 @@ struct MultiEngine {
     // ---- passes ---------------------------------------------------------------
     void step(bool adj, int it, unsigned sflags, unsigned vflags) {
         const ItemDesc* itm = adj ? d_items_a.as<ItemDesc>() : d_items_f.as<ItemDesc>();
+        const MultiMaps* mm = d_mmaps.as<MultiMaps>();
         int* err = d_err.as<int>();
         for (auto& gp : groups) {
             Group& g = *gp;
             const int k = active(g, it);
             if (k == 0) continue;
             const int ns = adj ? g.cum_a[k] : g.cum_f[k];
-            const int gs = std::max(1, std::min(ns, num_sms * (adj ? g.occ_a : g.occ_f)));
-            (adj ? g.ka.stress_a : g.kf.stress_f)(dim3(gs), stream, itm, (adj ? g.tiles_a : g.tiles_f).as<Tile>(),
-                                                  ns, it, sflags, err);
+            const bool tma_s = (adj ? g.tune.amap : g.tune.fmap) == 3;
+            if (tma_s) {
+                const dim3 gs((unsigned)std::max(1, std::min(ns, num_sms)));
+                (adj ? g.tm.adjoint : g.tm.stress)(gs, stream, mm, itm, (adj ? g.tiles_a : g.tiles_f).as<Tile>(), ns,
+                                                   it, sflags, 0, err);
+            } else {
+                const int gs = std::max(1, std::min(ns, num_sms * (adj ? g.occ_a : g.occ_f)));
+                (adj ? g.ka.stress_a : g.kf.stress_f)(dim3(gs), stream, itm,
+                                                      (adj ? g.tiles_a : g.tiles_f).as<Tile>(), ns, it, sflags, err);
+            }
             const int nv = g.cum_f[k];
-            const int gv = std::max(1, std::min(nv, num_sms * g.occ_v));
-            g.kf.velocity(dim3(gv), stream, itm, g.tiles_f.as<Tile>(), nv, it, vflags, err);
+            if (g.tune.fmap == 3) {
+                // source injection / recording of the active members in a small kernel after the pass
+                const unsigned ev = vflags & (FL_INJECT | FL_RECORD);
+                g.tm.velocity(dim3((unsigned)std::max(1, std::min(nv, num_sms))), stream, mm, itm,
+                              g.tiles_f.as<Tile>(), nv, it, vflags & ~ev, adj ? 1 : 0, err);
+                if (ev) {
+                    events_list_kernel<<<k, 256, 0, stream>>>(itm, d_gids.as<int>() + g.gid_off, it, ev);
+                    launches_now++;
+                }
+            } else {
+                const int gv = std::max(1, std::min(nv, num_sms * g.occ_v));
+                g.kf.velocity(dim3(gv), stream, itm, g.tiles_f.as<Tile>(), nv, it, vflags, err);
+            }
             launches_now += 2;
         }
     }
@@ -518,8 +613,22 @@ struct MultiEngine {
         CUDA_TRY(cudaEventCreate(&a));
         CUDA_TRY(cudaEventCreate(&b));
         const int k = (int)g.members.size();
+        const MultiMaps* mm = d_mmaps.as<MultiMaps>();
         auto launch = [&]() {
-            if (what == 0) {
+            if (what == 0 && g.tune.fmap == 3) {
+                const int ns = g.cum_f[k];
+                const dim3 gs((unsigned)std::max(1, std::min(ns, num_sms)));
+                g.tm.stress(gs, stream, mm, d_items_f.as<ItemDesc>(), g.tiles_f.as<Tile>(), ns, 0, 0u, 0,
+                            d_err.as<int>());
+                g.tm.velocity(gs, stream, mm, d_items_f.as<ItemDesc>(), g.tiles_f.as<Tile>(), ns, 0, 0u, 0,
+                              d_err.as<int>());
+                events_list_kernel<<<k, 256, 0, stream>>>(d_items_f.as<ItemDesc>(), d_gids.as<int>() + g.gid_off, 0,
+                                                          FL_INJECT);
+            } else if (what == 1 && g.tune.amap == 3) {
+                const int ns = g.cum_a[k];
+                g.tm.adjoint(dim3((unsigned)std::max(1, std::min(ns, num_sms))), stream, mm, d_items_a.as<ItemDesc>(),
+                             g.tiles_a.as<Tile>(), ns, 0, FL_GRAD, 0, d_err.as<int>());
+            } else if (what == 0) {
                 const int ns = g.cum_f[k];
                 g.kf.stress_f(dim3(std::max(1, std::min(ns, num_sms * g.occ_f))), stream, d_items_f.as<ItemDesc>(),
                               g.tiles_f.as<Tile>(), ns, 0, 0u, d_err.as<int>());
@@ -562,9 +671,11 @@ struct MultiEngine {
             TuneChoice best;
             best.fms = best.ams = 1e30;
             std::vector<std::pair<int, int>> fc, ac;
+            fc.push_back({3, 0});
             if (g.fp <= 4) fc.push_back({2, 0});
             fc.push_back({1, 0});
             for (int tz : {8, 16, 32, 64}) fc.push_back({0, tz});
+            ac.push_back({3, 0});
             ac.push_back({1, 0});
             for (int tz : {16, 32}) ac.push_back({0, tz});
             for (auto& f : fc) {
@@ -797,7 +908,8 @@ struct MultiEngine {
         stats = fwi_psv_stats{};
         stats.launches = launches_now;
         stats.forward_steps = nt_max;
-        stats.recompute_steps = recompute > 0 ? recompute : plan_cost;
+        (void)recompute;  // counted while the body runs; a graph replay runs the same plan
+        stats.recompute_steps = plan_recompute_steps(plan, nt_max, false);
         stats.adjoint_steps = nt_max;
         stats.device_bytes = (int64_t)(d_fwd.bytes + d_adj.bytes + d_snap.bytes + 4 * d_ws.bytes + d_grad.bytes +
                                        d_mat.bytes + 3 * d_rec.bytes);

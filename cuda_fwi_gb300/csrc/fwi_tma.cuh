@@ -307,13 +307,15 @@ __device__ __forceinline__ int strip_z(const ItemDesc& D, int iz, bool stress) {
 // ---------------------------------------------------------------------------
 // stress pass
 // ---------------------------------------------------------------------------
+// Copies of one tile into a stage: `desc` is the tile's slot descriptor, `b`
+// the slot coordinate of the 3-D state maps.
 template <int FP>
-__device__ __forceinline__ void stress_issue(const StressMaps& m, const ItemDesc* items, int b, int x0, int z0,
+__device__ __forceinline__ void stress_issue(const StressMaps& m, const ItemDesc* desc, int b, int x0, int z0,
                                              float* st, uint64_t* bar) {
     using G = TmaGeom<FP>;
     constexpr unsigned bytes = 4u * (2 * G::WX * G::WZ + 6 * G::CEN) + (unsigned)sizeof(ItemDesc);
     mbar_expect_tx(bar, bytes);
-    bulk_load(st + G::S_DESC, items + b, (unsigned)sizeof(ItemDesc), bar);
+    bulk_load(st + G::S_DESC, desc, (unsigned)sizeof(ItemDesc), bar);
     tma_load_3d(st, &m.vx, x0 - G::HX, z0 - FP, b, bar);
     tma_load_3d(st + G::HXZ, &m.vz, x0 - G::HX, z0 - FP, b, bar);
     float* c = st + 2 * G::HXZ;
@@ -488,13 +490,13 @@ __device__ __forceinline__ void stress_compute(const ItemDesc& D, const TmaGrid&
 // velocity pass (+ energy)
 // ---------------------------------------------------------------------------
 template <int FP>
-__device__ __forceinline__ void velocity_issue(const VelMaps& m, const ItemDesc* items, int b, int x0, int z0,
+__device__ __forceinline__ void velocity_issue(const VelMaps& m, const ItemDesc* desc, int b, int x0, int z0,
                                                float* st, uint64_t* bar, bool we) {
     using G = TmaGeom<FP>;
     const unsigned bytes = 4u * (G::WX * G::TZ + G::WX * G::WZ + G::TX * G::WZ + (we ? 5 : 4) * G::CEN) +
                            (unsigned)sizeof(ItemDesc);
     mbar_expect_tx(bar, bytes);
-    bulk_load(st + G::V_DESC, items + b, (unsigned)sizeof(ItemDesc), bar);
+    bulk_load(st + G::V_DESC, desc, (unsigned)sizeof(ItemDesc), bar);
     tma_load_3d(st, &m.sxx, x0 - G::HX, z0, b, bar);
     tma_load_3d(st + G::HXO, &m.szx, x0 - G::HX, z0 - FP, b, bar);
     tma_load_3d(st + G::HXO + G::HXZ, &m.szz, x0, z0 - FP, b, bar);
@@ -638,19 +640,19 @@ __device__ __forceinline__ void load_weights(const ItemDesc* items, float2 (&hx)
 // ---------------------------------------------------------------------------
 // persistent pipelined kernels
 // ---------------------------------------------------------------------------
-// Body shared by the passes.  ISSUE(b, x0, z0, stage_ptr, bar) queues the
-// copies of a tile; COMPUTE(tile, next, stage_ptr) runs its cells (tile and
-// next are (b, x0, z0) of this tile and of the CTA's next one, b = -1 when
-// there is none); TZ is the tile height.  The issuing thread writes each
-// tile's coordinates beside the barriers, so the other threads do no integer
-// division per tile.
+// Body shared by the passes.  COORDS(t, &b, &x0, &z0) names tile t of the
+// launch (b: its slot or model); ISSUE(b, x0, z0, stage_ptr, bar) queues its
+// copies; COMPUTE(tile, next, stage_ptr) runs its cells (tile and next are
+// (b, x0, z0) of this tile and of the CTA's next one, b = -1 when there is
+// none).  The issuing thread writes each tile's coordinates beside the
+// barriers, so the other threads do no integer division per tile.
 template <int STAGES>
 __host__ __device__ constexpr size_t tma_tail_bytes() {
     return STAGES * (sizeof(int4) + sizeof(uint64_t));
 }
 
-template <int FP, int STAGE_FLOATS, int TZ, class Issue, class Compute>
-__device__ __forceinline__ void tma_pipeline(const TmaGrid& g, int* err, Issue issue, Compute compute) {
+template <int FP, int STAGE_FLOATS, class Coords, class Issue, class Compute>
+__device__ __forceinline__ void tma_pipeline(int ntiles, int* err, Coords coords, Issue issue, Compute compute) {
     constexpr int kTmaStages = tma_stages<FP>();
     static_assert(STAGE_FLOATS % 32 == 0, "stages are 128-byte multiples");
     // dynamic shared memory only: the stages, the tile coordinates, the barriers
@@ -669,7 +671,7 @@ __device__ __forceinline__ void tma_pipeline(const TmaGrid& g, int* err, Issue i
     const int first = blockIdx.x, step = gridDim.x;
     auto issue_tile = [&](int t, int s) {
         int b, x0, z0;
-        tile_coords(g, t, &b, &x0, &z0, FP, TZ);
+        coords(t, &b, &x0, &z0);
         crd[s] = make_int4(b, x0, z0, 0);
         issue(b, x0, z0, tma_smem + s * STAGE_FLOATS, &bar[s]);
     };
@@ -678,19 +680,19 @@ __device__ __forceinline__ void tma_pipeline(const TmaGrid& g, int* err, Issue i
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         for (int s = 0; s < kTmaStages; s++) {
             const int t = first + s * step;
-            if (t < g.ntiles) issue_tile(t, s);
+            if (t < ntiles) issue_tile(t, s);
         }
     }
     __syncthreads();
     for (int k = 0;; k++) {
         const int t = first + k * step;
-        if (t >= g.ntiles) break;
+        if (t >= ntiles) break;
         const int s = k % kTmaStages;
         const unsigned parity = (unsigned)((k / kTmaStages) & 1);
         const bool ok = mbar_wait_bounded(&bar[s], parity);
         if (ok) {
             // coordinates of this thread's next tile (issued already: stages >= 2)
-            const int4 nx = first + (k + 1) * step < g.ntiles ? crd[(k + 1) % kTmaStages] : make_int4(-1, 0, 0, 0);
+            const int4 nx = first + (k + 1) * step < ntiles ? crd[(k + 1) % kTmaStages] : make_int4(-1, 0, 0, 0);
             compute(crd[s], nx, tma_smem + s * STAGE_FLOATS);
         }
         // every thread is done with stage s (or some thread's wait gave up)
@@ -700,14 +702,14 @@ __device__ __forceinline__ void tma_pipeline(const TmaGrid& g, int* err, Issue i
                 // drain the copies this CTA issued and has not consumed (bounded)
                 for (int j = k; j < k + kTmaStages; j++) {
                     const int tj = first + j * step;
-                    if (tj < g.ntiles) mbar_wait_bounded(&bar[j % kTmaStages], (unsigned)((j / kTmaStages) & 1));
+                    if (tj < ntiles) mbar_wait_bounded(&bar[j % kTmaStages], (unsigned)((j / kTmaStages) & 1));
                 }
             }
             return;
         }
         if (tid == 0) {
             const int tn = first + (k + kTmaStages) * step;
-            if (tn < g.ntiles) {
+            if (tn < ntiles) {
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                 issue_tile(tn, s);
             }
@@ -733,9 +735,11 @@ __global__ void __launch_bounds__(kTmaThreads, 1)
     using G = TmaGeom<FP>;
     float2 hx[FP], hz[FP];
     load_weights<FP>(items, hx, hz);
-    tma_pipeline<FP, G::S_STAGE, kTmaTZ>(
-        g, err,
-        [&](int b, int x0, int z0, float* st, uint64_t* bar) { stress_issue<FP>(maps, items, b, x0, z0, st, bar); },
+    tma_pipeline<FP, G::S_STAGE>(
+        g.ntiles, err, [&](int t, int* b, int* x0, int* z0) { tile_coords(g, t, b, x0, z0, FP, kTmaTZ); },
+        [&](int b, int x0, int z0, float* st, uint64_t* bar) {
+            stress_issue<FP>(maps, items + b, b, x0, z0, st, bar);
+        },
         [&](int4 c, int4, const float* st) {
             stress_compute<FP>(*reinterpret_cast<const ItemDesc*>(st + G::S_DESC), g, st, c.y, c.z, it, flags, hx,
                                hz);
@@ -750,10 +754,10 @@ __global__ void __launch_bounds__(kTmaThreads, 1)
     const bool we = (flags & FL_WE) != 0;
     float2 hx[FP], hz[FP];
     load_weights<FP>(items, hx, hz);
-    tma_pipeline<FP, G::V_STAGE, kTmaTZ>(
-        g, err,
+    tma_pipeline<FP, G::V_STAGE>(
+        g.ntiles, err, [&](int t, int* b, int* x0, int* z0) { tile_coords(g, t, b, x0, z0, FP, kTmaTZ); },
         [&](int b, int x0, int z0, float* st, uint64_t* bar) {
-            velocity_issue<FP>(maps, items, b, x0, z0, st, bar, we);
+            velocity_issue<FP>(maps, items + b, b, x0, z0, st, bar, we);
         },
         [&](int4 c, int4, const float* st) {
             velocity_compute<FP>(*reinterpret_cast<const ItemDesc*>(st + G::V_DESC), g, st, c.y, c.z, flags, hx, hz);
@@ -794,12 +798,12 @@ __host__ __device__ constexpr size_t adjoint_tma_smem() {
 static_assert(adjoint_tma_smem<4>() <= 232448 && adjoint_tma_smem<6>() <= 232448, "shared memory per CTA");
 
 template <int FP>
-__device__ __forceinline__ void adjoint_issue(const AdjMaps& m, const ItemDesc* items, int b, int x0, int z0,
+__device__ __forceinline__ void adjoint_issue(const AdjMaps& m, const ItemDesc* desc, int b, int x0, int z0,
                                               float* st, uint64_t* bar, bool grad) {
     using G = AdjGeom<FP>;
     const unsigned bytes = 4u * (2 * G::WX * G::WZ + (grad ? 13 : 8) * G::CEN) + (unsigned)sizeof(ItemDesc);
     mbar_expect_tx(bar, bytes);
-    bulk_load(st + G::DESC, items + b, (unsigned)sizeof(ItemDesc), bar);
+    bulk_load(st + G::DESC, desc, (unsigned)sizeof(ItemDesc), bar);
     tma_load_3d(st, &m.vx, x0 - G::HX, z0 - FP, b, bar);
     tma_load_3d(st + G::HXZ, &m.vz, x0 - G::HX, z0 - FP, b, bar);
     float* c = st + 2 * G::HXZ;
@@ -1041,10 +1045,10 @@ __global__ void __launch_bounds__(kTmaThreads, 1)
     const int wx1 = __ldg(&items[0].wx1), wz1 = __ldg(&items[0].wz1), nfx = __ldg(&items[0].nfx);
     GradAhead ga;
     ga.valid = false;
-    tma_pipeline<FP, G::STAGE, kAdjTZ>(
-        g, err,
+    tma_pipeline<FP, G::STAGE>(
+        g.ntiles, err, [&](int t, int* b, int* x0, int* z0) { tile_coords(g, t, b, x0, z0, FP, kAdjTZ); },
         [&](int b, int x0, int z0, float* st, uint64_t* bar) {
-            adjoint_issue<FP>(maps, items, b, x0, z0, st, bar, grad);
+            adjoint_issue<FP>(maps, items + b, b, x0, z0, st, bar, grad);
         },
         [&](int4 c, int4 n, const float* st) {
             const ItemDesc& D = *reinterpret_cast<const ItemDesc*>(st + G::DESC);
@@ -1071,6 +1075,140 @@ __global__ void __launch_bounds__(kTmaThreads, 1)
                 ga.g[4] = gr[gi];
                 ga.g[5] = gr[gi + 1];
                 ga.valid = true;
+            }
+        });
+}
+
+// ---------------------------------------------------------------------------
+// independent models of uneven size in one launch (multi-model engine)
+// ---------------------------------------------------------------------------
+// Per model, the tensor maps of its states (one slot each) live in device
+// memory, written by the host before the launches, and the TMA copies take
+// them by address.  The tile work-list gives (model, x0, z0); the stencil
+// weights and the plain-stencil ranges come from the model's staged
+// descriptor.  Models of one half order share a launch.
+struct MultiMaps {
+    StressMaps sf;  // forward state, stress pass
+    VelMaps vf;     // forward state, velocity pass (energy Ws)
+    VelMaps va;     // adjoint state, velocity pass (energy Wr)
+    AdjMaps a;      // adjoint stress pass: adjoint state, ux/uz, forward fields
+};
+
+// Plain-stencil ranges of one model: the rule the single-model engine applies
+// on the host for its TmaGrid.
+__device__ __forceinline__ TmaGrid model_ranges(const ItemDesc& D) {
+    TmaGrid g{};
+    const int fp = D.fpad;
+    g.cxl = fp;
+    g.cxh = D.nxt - fp - 1;
+    g.czl = fp;
+    g.czh = D.nzt - fp - 1;
+    if (D.npml > 0) {
+        g.cxl = max(g.cxl, D.ppad + 1);
+        g.cxh = min(g.cxh, D.nxt - D.ppad - 2);
+        g.czh = min(g.czh, D.nzt - D.ppad - 2);
+        if (!D.fsurf) g.czl = max(g.czl, D.ppad + 1);
+    }
+    if (D.fsurf) g.czl = max(g.czl, 2 * fp + 1);
+    g.gxl = g.gzl = 0;
+    g.gxh = g.gzh = -1;
+    if (D.fwi_dx == 1 && D.fwi_dz == 1) {
+        g.gxl = D.wx1;
+        g.gxh = D.wx2 - 1;
+        g.gzl = D.wz1;
+        g.gzh = D.wz2 - 1;
+    }
+    return g;
+}
+
+template <int FP>
+__device__ __forceinline__ void staged_weights(const ItemDesc& D, float2 (&hx)[FP], float2 (&hz)[FP]) {
+#pragma unroll
+    for (int k = 0; k < FP; k++) {
+        hx[k] = bc2(D.hx[k]);
+        hz[k] = bc2(D.hz[k]);
+    }
+}
+
+template <int FP>
+__global__ void __launch_bounds__(kTmaThreads, 1)
+    stress_tma_multi_kernel(const MultiMaps* __restrict__ maps, const ItemDesc* __restrict__ items,
+                            const Tile* __restrict__ tiles, int ntiles, int it, unsigned flags, int* err) {
+    using G = TmaGeom<FP>;
+    tma_pipeline<FP, G::S_STAGE>(
+        ntiles, err,
+        [&](int t, int* b, int* x0, int* z0) {
+            const Tile T = tiles[t];
+            *b = T.item;
+            *x0 = T.x0;
+            *z0 = T.z0;
+        },
+        [&](int b, int x0, int z0, float* st, uint64_t* bar) {
+            stress_issue<FP>(maps[b].sf, items + b, 0, x0, z0, st, bar);
+        },
+        [&](int4 c, int4, const float* st) {
+            const ItemDesc& D = *reinterpret_cast<const ItemDesc*>(st + G::S_DESC);
+            float2 hx[FP], hz[FP];
+            staged_weights<FP>(D, hx, hz);
+            stress_compute<FP>(D, model_ranges(D), st, c.y, c.z, it, flags, hx, hz);
+        });
+}
+
+template <int FP>
+__global__ void __launch_bounds__(kTmaThreads, 1)
+    velocity_tma_multi_kernel(const MultiMaps* __restrict__ maps, const ItemDesc* __restrict__ items,
+                              const Tile* __restrict__ tiles, int ntiles, int it, unsigned flags, int adj, int* err) {
+    using G = TmaGeom<FP>;
+    const bool we = (flags & FL_WE) != 0;
+    tma_pipeline<FP, G::V_STAGE>(
+        ntiles, err,
+        [&](int t, int* b, int* x0, int* z0) {
+            const Tile T = tiles[t];
+            *b = T.item;
+            *x0 = T.x0;
+            *z0 = T.z0;
+        },
+        [&](int b, int x0, int z0, float* st, uint64_t* bar) {
+            velocity_issue<FP>(adj ? maps[b].va : maps[b].vf, items + b, 0, x0, z0, st, bar, we);
+        },
+        [&](int4 c, int4, const float* st) {
+            const ItemDesc& D = *reinterpret_cast<const ItemDesc*>(st + G::V_DESC);
+            float2 hx[FP], hz[FP];
+            staged_weights<FP>(D, hx, hz);
+            velocity_compute<FP>(D, model_ranges(D), st, c.y, c.z, flags, hx, hz);
+        });
+}
+
+template <int FP>
+__global__ void __launch_bounds__(kTmaThreads, 1)
+    adjoint_tma_multi_kernel(const MultiMaps* __restrict__ maps, const ItemDesc* __restrict__ items,
+                             const Tile* __restrict__ tiles, int ntiles, int it, unsigned flags, int* err) {
+    using G = AdjGeom<FP>;
+    const bool grad = (flags & FL_GRAD) != 0;
+    GradAhead none;
+    none.valid = false;
+    tma_pipeline<FP, G::STAGE>(
+        ntiles, err,
+        [&](int t, int* b, int* x0, int* z0) {
+            const Tile T = tiles[t];
+            *b = T.item;
+            *x0 = T.x0;
+            *z0 = T.z0;
+        },
+        [&](int b, int x0, int z0, float* st, uint64_t* bar) {
+            adjoint_issue<FP>(maps[b].a, items + b, 0, x0, z0, st, bar, grad);
+        },
+        [&](int4 c, int4, const float* st) {
+            const ItemDesc& D = *reinterpret_cast<const ItemDesc*>(st + G::DESC);
+            float2 hx[FP], hz[FP];
+            staged_weights<FP>(D, hx, hz);
+            const bool in = interior_warp_adj(model_ranges(D), c.y, c.z, grad);
+            if (grad) {
+                if (in) adjoint_rows<FP, true, true>(D, st, c.y, c.z, hx, hz, none);
+                else adjoint_rows<FP, false, true>(D, st, c.y, c.z, hx, hz, none);
+            } else {
+                if (in) adjoint_rows<FP, true, false>(D, st, c.y, c.z, hx, hz, none);
+                else adjoint_rows<FP, false, false>(D, st, c.y, c.z, hx, hz, none);
             }
         });
 }

@@ -17,7 +17,7 @@ from . import _capi
 from ._capi import check, pd, pi
 from .problem import Problem
 
-MAPPINGS = {0: "z-march", 1: "scalar cells", 2: "vectorised cells"}
+MAPPINGS = {0: "z-march", 1: "scalar cells", 2: "vectorised cells", 3: "TMA-staged tiles"}
 
 
 def _f64(a):

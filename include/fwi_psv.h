@@ -381,7 +381,8 @@ int fwi_psv_multi_gradient(fwi_psv_multi* m, const double* const* obs, double* m
  * info = {half order, models, forward mapping, forward tile rows, adjoint mapping,
  * adjoint tile rows, read from the cache (1) or timed now (0)}; ms = {forward pair,
  * adjoint stress} per launch over the whole group, as timed when the choice was made
- * (the cache keeps them).  Mappings: 0 z-march (tile rows), 1 scalar cells, 2 vectorised cells. */
+ * (the cache keeps them).  Mappings: 0 z-march (tile rows), 1 scalar cells, 2 vectorised cells,
+ * 3 TMA-staged tiles (tensor maps per model in device memory). */
 int fwi_psv_multi_tuning(fwi_psv_multi* m, int group, int info[7], double ms[2]);
 int fwi_psv_multi_get_stats(fwi_psv_multi* m, fwi_psv_stats* out);
 

@@ -90,3 +90,29 @@ def test_graphs_mappings_and_cache(tune_cache):
     for k in range(len(ps)):
         for i in range(3):
             assert rel_l2(g3[k][i], g1[k][i]) <= 3e-5, (k, i)
+
+
+def test_tma_tiles_match_oracle(tune_cache):
+    """The TMA-staged passes over the uneven work-list (maps per model in device
+    memory): the tuner's cache is rewritten to choose them for both passes of
+    every order group, and a new engine reads it."""
+    ps, obs = _models()
+    with MultiEngine(ps, snapshots=5, autotune=True) as m:
+        m.gradient(obs)
+    data = json.loads(tune_cache.read_text())
+    for v in data.values():
+        v.update(fwd_map=3, fwd_tz=0, adj_map=3, adj_tz=0)
+    # the engine's layout: one entry per line
+    lines = [f" {json.dumps(k)}: {json.dumps(v)}" for k, v in data.items()]
+    tune_cache.write_text("{\n" + ",\n".join(lines) + "\n}\n")
+    with MultiEngine(ps, snapshots=5, autotune=True) as m:
+        grads, mis = m.gradient(obs)
+        tun = m.tuning()
+        grads_r, mis_r = m.gradient(obs)  # graph replay
+    assert all(t["cached"] and t["forward_mapping"] == t["adjoint_mapping"] == "TMA-staged tiles" for t in tun)
+    for k, p in enumerate(ps):
+        J, g_o, _, _ = O.gradient(p, obs[k], 0)
+        assert mis[k] == pytest.approx(J, rel=1e-4), k
+        for i in range(3):
+            assert rel_l2(grads[k][i], _oracle_grid(p, g_o[i])) <= 1e-4, (k, i)
+            assert np.array_equal(grads[k][i], grads_r[k][i])
