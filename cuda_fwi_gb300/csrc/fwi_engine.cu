@@ -412,27 +412,31 @@ static long long plan_recompute_steps(const std::vector<Action>& plan, int n, bo
 
 // TMA-staged passes over a work-list of tiles of several models (the
 // multi-model engine; maps per model in device memory).
-using TmaMultiFn = void (*)(dim3, cudaStream_t, const MultiMaps*, const ItemDesc*, const Tile*, int, int, unsigned,
-                            int, int*);
+// Arguments: maps of the source and destination buffers, descriptors writing
+// to the destination, tiles, count, step, flags, adjoint state (velocity
+// pass), CPML-memory offset source - destination (floats), error word.
+using TmaMultiFn = void (*)(dim3, cudaStream_t, const MultiMaps*, const MultiMaps*, const ItemDesc*, const Tile*, int,
+                            int, unsigned, int, long long, int*);
 struct TmaMultiSet {
-    TmaMultiFn stress, velocity, adjoint;  // velocity: int argument = adjoint state
+    TmaMultiFn stress, velocity, adjoint;
     cudaError_t (*prepare)();
 };
 template <int FP>
-static void tm_stress(dim3 g, cudaStream_t s, const MultiMaps* m, const ItemDesc* it, const Tile* t, int nt, int step,
-                      unsigned flags, int, int* err) {
-    stress_tma_multi_kernel<FP><<<g, kTmaThreads, stress_tma_smem<FP>(), s>>>(m, it, t, nt, step, flags, err);
+static void tm_stress(dim3 g, cudaStream_t s, const MultiMaps* mx, const MultiMaps* my, const ItemDesc* it,
+                      const Tile* t, int nt, int step, unsigned flags, int, long long msrc, int* err) {
+    stress_tma_multi_kernel<FP><<<g, kTmaThreads, stress_tma_smem<FP>(), s>>>(mx, my, it, t, nt, step, flags, msrc,
+                                                                                 err);
 }
 template <int FP>
-static void tm_velocity(dim3 g, cudaStream_t s, const MultiMaps* m, const ItemDesc* it, const Tile* t, int nt,
-                        int step, unsigned flags, int adj, int* err) {
-    velocity_tma_multi_kernel<FP><<<g, kTmaThreads, velocity_tma_smem<FP>(), s>>>(m, it, t, nt, step, flags, adj,
-                                                                                     err);
+static void tm_velocity(dim3 g, cudaStream_t s, const MultiMaps* mx, const MultiMaps* my, const ItemDesc* it,
+                        const Tile* t, int nt, int step, unsigned flags, int adj, long long msrc, int* err) {
+    velocity_tma_multi_kernel<FP><<<g, kTmaThreads, velocity_tma_smem<FP>(), s>>>(mx, my, it, t, nt, step, flags,
+                                                                                     adj, msrc, err);
 }
 template <int FP>
-static void tm_adjoint(dim3 g, cudaStream_t s, const MultiMaps* m, const ItemDesc* it, const Tile* t, int nt,
-                       int step, unsigned flags, int, int* err) {
-    adjoint_tma_multi_kernel<FP><<<g, kTmaThreads, adjoint_tma_smem<FP>(), s>>>(m, it, t, nt, step, flags, err);
+static void tm_adjoint(dim3 g, cudaStream_t s, const MultiMaps* mx, const MultiMaps*, const ItemDesc* it,
+                       const Tile* t, int nt, int step, unsigned flags, int, long long, int* err) {
+    adjoint_tma_multi_kernel<FP><<<g, kTmaThreads, adjoint_tma_smem<FP>(), s>>>(mx, it, t, nt, step, flags, err);
 }
 template <int FP>
 static cudaError_t tm_prepare() {

@@ -60,6 +60,11 @@ struct MultiEngine {
     DBuf d_rowmis, d_blow, d_snap, d_items_f, d_items_a, d_evcol, d_ev, d_evx, d_err, d_rows;
     DBuf d_mmaps, d_gids;   // TMA maps per model; member lists of the groups (events)
     bool mmaps_built = false;
+    // Copy-free checkpointing (every group on the TMA tiles): buffer k < slots
+    // is checkpoint memory, buffer `slots` is d_fwd; per buffer and model the
+    // maps of that buffer's forward state and descriptors writing to it.
+    DBuf d_mmaps_b, d_items_b;
+    int mmaps_b_slots = -1;
     struct Group {
         int fp = 0;
         std::vector<int> members;  // item indices, nt descending
@@ -303,6 +308,33 @@ struct MultiEngine {
         return FWI_OK;
     }
 
+    // The maps of a model's forward state held at fwd_base (+ its offset):
+    // the stress pass, the velocity pass and the adjoint pass's forward fields.
+    int forward_maps(MultiMaps& M, int b, float* fwd_base) {
+        const MultiItem& I = items[b];
+        const int FPv = I.fpad, hx = (FPv + 3) / 4 * 4;
+        const int wx = kTmaTX + 2 * hx, wz = kTmaTZ + 2 * FPv;
+        const size_t rb = (size_t)I.pitch * 4, sb = I.state * 4, f = I.field;
+        float* sf = fwd_base + I.off_state;
+        const int X = I.nxt, Z = I.nzt;
+        FWI_TRY(make_map(&M.sf.vx, sf + F_VX * f, X, Z, 1, rb, sb, wx, wz));
+        FWI_TRY(make_map(&M.sf.vz, sf + F_VZ * f, X, Z, 1, rb, sb, wx, wz));
+        FWI_TRY(make_map(&M.sf.sxx, sf + F_SXX * f, X, Z, 1, rb, sb, kTmaTX, kTmaTZ));
+        FWI_TRY(make_map(&M.sf.szx, sf + F_SZX * f, X, Z, 1, rb, sb, kTmaTX, kTmaTZ));
+        FWI_TRY(make_map(&M.sf.szz, sf + F_SZZ * f, X, Z, 1, rb, sb, kTmaTX, kTmaTZ));
+        FWI_TRY(make_map(&M.vf.sxx, sf + F_SXX * f, X, Z, 1, rb, sb, wx, kTmaTZ));
+        FWI_TRY(make_map(&M.vf.szx, sf + F_SZX * f, X, Z, 1, rb, sb, wx, wz));
+        FWI_TRY(make_map(&M.vf.szz, sf + F_SZZ * f, X, Z, 1, rb, sb, kTmaTX, wz));
+        FWI_TRY(make_map(&M.vf.vx, sf + F_VX * f, X, Z, 1, rb, sb, kTmaTX, kTmaTZ));
+        FWI_TRY(make_map(&M.vf.vz, sf + F_VZ * f, X, Z, 1, rb, sb, kTmaTX, kTmaTZ));
+        FWI_TRY(make_map(&M.a.fvx, sf + F_VX * f, X, Z, 1, rb, sb, kTmaTX, kAdjTZ));
+        FWI_TRY(make_map(&M.a.fvz, sf + F_VZ * f, X, Z, 1, rb, sb, kTmaTX, kAdjTZ));
+        FWI_TRY(make_map(&M.a.fsxx, sf + F_SXX * f, X, Z, 1, rb, sb, kTmaTX, kAdjTZ));
+        FWI_TRY(make_map(&M.a.fszx, sf + F_SZX * f, X, Z, 1, rb, sb, kTmaTX, kAdjTZ));
+        FWI_TRY(make_map(&M.a.fszz, sf + F_SZZ * f, X, Z, 1, rb, sb, kTmaTX, kAdjTZ));
+        return FWI_OK;
+    }
+
     // Tensor maps of every model's states for the TMA-staged passes (one slot
     // per map; addresses are fixed for the engine's lifetime).
     int build_mmaps() {
@@ -362,7 +394,7 @@ struct MultiEngine {
         return FWI_OK;
     }
 
-    void fill_item(ItemDesc& d, int b, bool adj) {
+    void fill_item(ItemDesc& d, int b, bool adj, float* fwd_base = nullptr) {
         const MultiItem& I = items[b];
         std::memset(&d, 0, sizeof d);
         d.nzt = I.nzt; d.nxt = I.nxt; d.pitch = I.pitch; d.fpad = I.fpad;
@@ -380,7 +412,7 @@ struct MultiEngine {
         d.cpml = d_cpml.as<float>() + I.off_cpml;
         const float* mt = d_mat.as<float>() + I.off_mat;
         d.L = mt; d.M2 = mt + I.field; d.MZX = mt + 2 * I.field; d.BX = mt + 3 * I.field; d.BZ = mt + 4 * I.field;
-        float* st = (adj ? d_adj.as<float>() : d_fwd.as<float>()) + I.off_state;
+        float* st = (adj ? d_adj.as<float>() : fwd_base ? fwd_base : d_fwd.as<float>()) + I.off_state;
         d.vx = st + F_VX * I.field; d.vz = st + F_VZ * I.field; d.sxx = st + F_SXX * I.field;
         d.szx = st + F_SZX * I.field; d.szz = st + F_SZZ * I.field;
         float* cp = st + 5 * I.field;
@@ -444,6 +476,110 @@ struct MultiEngine {
         return FWI_OK;
     }
 
+    bool copy_free() const {
+        if (slots <= 0) return false;
+        for (auto& g : groups)
+            if (g->tune.fmap != 3 || g->tune.amap != 3) return false;
+        return true;
+    }
+    float* buf(int k) { return k < slots ? snap(k) : d_fwd.as<float>(); }
+    // per-buffer maps and descriptors of the copy-free plan (rebuilt when the
+    // slot count or the checkpoint memory changes)
+    int build_buffers() {
+        if (mmaps_b_slots == slots) return FWI_OK;
+        FWI_TRY(build_mmaps());
+        std::vector<MultiMaps> base(n);
+        CUDA_TRY(cudaMemcpy(base.data(), d_mmaps.p, n * sizeof(MultiMaps), cudaMemcpyDeviceToHost));
+        const int nbuf = slots + 1;
+        std::vector<MultiMaps> mm((size_t)nbuf * n);
+        std::vector<ItemDesc> it((size_t)nbuf * n);
+        for (int k = 0; k < nbuf; k++)
+            for (int b = 0; b < n; b++) {
+                MultiMaps& M = mm[(size_t)k * n + b];
+                M = base[b];
+                FWI_TRY(forward_maps(M, b, buf(k)));
+                fill_item(it[(size_t)k * n + b], b, false, buf(k));
+            }
+        drop_graphs();
+        FWI_TRY(d_mmaps_b.ensure(mm.size() * sizeof(MultiMaps)));
+        FWI_TRY(d_items_b.ensure(it.size() * sizeof(ItemDesc)));
+        CUDA_TRY(cudaMemcpy(d_mmaps_b.p, mm.data(), mm.size() * sizeof(MultiMaps), cudaMemcpyHostToDevice));
+        CUDA_TRY(cudaMemcpy(d_items_b.p, it.data(), it.size() * sizeof(ItemDesc), cudaMemcpyHostToDevice));
+        mmaps_b_slots = slots;
+        return FWI_OK;
+    }
+    // One recompute step of every active model from buffer x into buffer y
+    // (x == y: in place); see the single-model engine's step_bufs.
+    void step_bufs(int x, int y, int it) {
+        const MultiMaps* mx = d_mmaps_b.as<MultiMaps>() + (size_t)x * n;
+        const MultiMaps* my = d_mmaps_b.as<MultiMaps>() + (size_t)y * n;
+        const ItemDesc* itm = d_items_b.as<ItemDesc>() + (size_t)y * n;
+        const long long msrc = (long long)(buf(x) - buf(y));
+        int* err = d_err.as<int>();
+        for (auto& gp : groups) {
+            Group& g = *gp;
+            const int k = active(g, it);
+            if (k == 0) continue;
+            const int ns = g.cum_f[k];
+            const dim3 gs((unsigned)std::max(1, std::min(ns, num_sms)));
+            g.tm.stress(gs, stream, mx, my, itm, g.tiles_f.as<Tile>(), ns, it, 0u, 0, msrc, err);
+            g.tm.velocity(gs, stream, mx, my, itm, g.tiles_f.as<Tile>(), ns, it, 0u, 0, msrc, err);
+            events_list_kernel<<<k, 256, 0, stream>>>(itm, d_gids.as<int>() + g.gid_off, it, FL_INJECT);
+            launches_now += 3;
+        }
+    }
+    // The plan from action k on without state copies (the single-model
+    // engine's run_plan_copy_free): RESTORE points at the slot's buffer, the
+    // next ADVANCE steps out of it, SAVE swaps the working buffer with the
+    // slot's free one, ADJOINT reads the forward fields from the buffer that
+    // holds them.
+    int run_plan_copy_free(size_t k, int last_slot, int last_state, long long* recompute) {
+        std::vector<int> phys(slots);
+        for (int i = 0; i < slots; i++) phys[i] = i;
+        int wb = slots;
+        int src = last_slot >= 0 ? phys[last_slot] : wb;
+        if (last_slot < 0) CUDA_TRY(cudaMemsetAsync(buf(wb), 0, total_state * 4, stream));
+        auto advance = [&](int t0, int t1) {
+            for (int it = t0; it < t1; it++) {
+                step_bufs(src, wb, it);
+                src = wb;
+            }
+            *recompute += std::max(0, t1 - t0);
+        };
+        advance(last_state, nt_max - 1);
+        for (; k < plan.size(); k++) {
+            const Action& a = plan[k];
+            switch (a.kind) {
+                case Action::ADVANCE:
+                    advance(a.a, a.b);
+                    break;
+                case Action::SAVE:
+                    if (src == wb) {
+                        std::swap(phys[a.a], wb);
+                    } else {
+                        FWI_TRY(state_copy(buf(phys[a.a]), buf(src)));
+                    }
+                    src = phys[a.a];
+                    break;
+                case Action::RESTORE:
+                    if (a.a < 0) {
+                        CUDA_TRY(cudaMemsetAsync(buf(wb), 0, total_state * 4, stream));
+                        src = wb;
+                    } else {
+                        src = phys[a.a];
+                    }
+                    break;
+                case Action::ADJOINT:
+                    adj_src = d_mmaps_b.as<MultiMaps>() + (size_t)src * n;
+                    step(true, a.a, FL_GRAD, FL_INJECT | FL_WE);
+                    adj_src = nullptr;
+                    break;
+            }
+        }
+        return FWI_OK;
+    }
+    const MultiMaps* adj_src = nullptr;  // maps naming the forward state of the adjoint pass (null: d_fwd's)
+
     // number of members of g still running at time step it
     int active(const Group& g, int it) const {
         int k = 0;
@@ -464,8 +600,9 @@ struct MultiEngine {
             const bool tma_s = (adj ? g.tune.amap : g.tune.fmap) == 3;
             if (tma_s) {
                 const dim3 gs((unsigned)std::max(1, std::min(ns, num_sms)));
-                (adj ? g.tm.adjoint : g.tm.stress)(gs, stream, mm, itm, (adj ? g.tiles_a : g.tiles_f).as<Tile>(), ns,
-                                                   it, sflags, 0, err);
+                const MultiMaps* ms = adj && adj_src ? adj_src : mm;
+                (adj ? g.tm.adjoint : g.tm.stress)(gs, stream, ms, ms, itm, (adj ? g.tiles_a : g.tiles_f).as<Tile>(),
+                                                   ns, it, sflags, 0, 0, err);
             } else {
                 const int gs = std::max(1, std::min(ns, num_sms * (adj ? g.occ_a : g.occ_f)));
                 (adj ? g.ka.stress_a : g.kf.stress_f)(dim3(gs), stream, itm,
@@ -475,8 +612,8 @@ struct MultiEngine {
             if (g.tune.fmap == 3) {
                 // source injection / recording of the active members in a small kernel after the pass
                 const unsigned ev = vflags & (FL_INJECT | FL_RECORD);
-                g.tm.velocity(dim3((unsigned)std::max(1, std::min(nv, num_sms))), stream, mm, itm,
-                              g.tiles_f.as<Tile>(), nv, it, vflags & ~ev, adj ? 1 : 0, err);
+                g.tm.velocity(dim3((unsigned)std::max(1, std::min(nv, num_sms))), stream, mm, mm, itm,
+                              g.tiles_f.as<Tile>(), nv, it, vflags & ~ev, adj ? 1 : 0, 0, err);
                 if (ev) {
                     events_list_kernel<<<k, 256, 0, stream>>>(itm, d_gids.as<int>() + g.gid_off, it, ev);
                     launches_now++;
@@ -618,16 +755,16 @@ struct MultiEngine {
             if (what == 0 && g.tune.fmap == 3) {
                 const int ns = g.cum_f[k];
                 const dim3 gs((unsigned)std::max(1, std::min(ns, num_sms)));
-                g.tm.stress(gs, stream, mm, d_items_f.as<ItemDesc>(), g.tiles_f.as<Tile>(), ns, 0, 0u, 0,
+                g.tm.stress(gs, stream, mm, mm, d_items_f.as<ItemDesc>(), g.tiles_f.as<Tile>(), ns, 0, 0u, 0, 0,
                             d_err.as<int>());
-                g.tm.velocity(gs, stream, mm, d_items_f.as<ItemDesc>(), g.tiles_f.as<Tile>(), ns, 0, 0u, 0,
+                g.tm.velocity(gs, stream, mm, mm, d_items_f.as<ItemDesc>(), g.tiles_f.as<Tile>(), ns, 0, 0u, 0, 0,
                               d_err.as<int>());
                 events_list_kernel<<<k, 256, 0, stream>>>(d_items_f.as<ItemDesc>(), d_gids.as<int>() + g.gid_off, 0,
                                                           FL_INJECT);
             } else if (what == 1 && g.tune.amap == 3) {
                 const int ns = g.cum_a[k];
-                g.tm.adjoint(dim3((unsigned)std::max(1, std::min(ns, num_sms))), stream, mm, d_items_a.as<ItemDesc>(),
-                             g.tiles_a.as<Tile>(), ns, 0, FL_GRAD, 0, d_err.as<int>());
+                g.tm.adjoint(dim3((unsigned)std::max(1, std::min(ns, num_sms))), stream, mm, mm,
+                             d_items_a.as<ItemDesc>(), g.tiles_a.as<Tile>(), ns, 0, FL_GRAD, 0, 0, d_err.as<int>());
             } else if (what == 0) {
                 const int ns = g.cum_f[k];
                 g.kf.stress_f(dim3(std::max(1, std::min(ns, num_sms * g.occ_f))), stream, d_items_f.as<ItemDesc>(),
@@ -762,8 +899,14 @@ struct MultiEngine {
         if (want != slots || plan.empty()) {
             slots = want;
             if (slots > 0) {
-                if (d_snap.bytes < (size_t)slots * total_state * 4) drop_graphs();
-                FWI_TRY(d_snap.ensure((size_t)slots * total_state * 4));
+                if (d_snap.bytes < (size_t)slots * total_state * 4) {
+                    drop_graphs();
+                    FWI_TRY(d_snap.ensure((size_t)slots * total_state * 4));
+                    // the copy-free plan steps into any checkpoint buffer: cells that
+                    // no pass writes (grid borders) must read as zero there too
+                    CUDA_TRY(cudaMemset(d_snap.p, 0, (size_t)slots * total_state * 4));
+                    mmaps_b_slots = -1;
+                }
             }
             plan = plan_binomial(nt_max, slots, &plan_cost);
             drop_graphs();
@@ -779,6 +922,8 @@ struct MultiEngine {
             CUDA_TRY(cudaMemcpyAsync(d_obs.p, h.data(), total_rec * 4, cudaMemcpyHostToDevice, stream));
             CUDA_TRY(cudaStreamSynchronize(stream));
         }
+        const bool cfree = copy_free();
+        if (cfree) FWI_TRY(build_buffers());
         cudaEvent_t e0, e1;
         CUDA_TRY(cudaEventCreate(&e0));
         CUDA_TRY(cudaEventCreate(&e1));
@@ -789,7 +934,7 @@ struct MultiEngine {
             if (a.kind == Action::ADJOINT) break;
             if (a.kind == Action::SAVE) saves.push_back({a.b, a.a});
         }
-        const std::string sk = "|s" + std::to_string(slots);
+        const std::string sk = "|s" + std::to_string(slots) + (cfree ? "|cf" : "");
         FWI_TRY(run_phase("fwd" + sk, [&]() -> int {
             CUDA_TRY(cudaMemsetAsync(d_fwd.p, 0, total_state * 4, stream));
             CUDA_TRY(cudaMemsetAsync(d_ws.p, 0, total_field * 4, stream));
@@ -843,6 +988,7 @@ struct MultiEngine {
                 }
                 k++;
             }
+            if (cfree) return run_plan_copy_free(k, last_slot, last_state, &recompute);
             if (last_slot >= 0) FWI_TRY(state_copy(d_fwd.as<float>(), snap(last_slot)));
             else CUDA_TRY(cudaMemsetAsync(d_fwd.p, 0, total_state * 4, stream));
             forward_steps(last_state, nt_max - 1, false);

@@ -508,6 +508,28 @@ __device__ __forceinline__ void velocity_issue(const VelMaps& m, const ItemDesc*
     if (we) tma_load_3d(c + 4 * G::CEN, &m.We, x0, z0, b, bar);
 }
 
+// The same with the stresses from `ms` and velocities, buoyancies and energy
+// from `mv` (a step out of one state buffer into another: the stresses were
+// just written to the destination, the velocities are still in the source).
+template <int FP>
+__device__ __forceinline__ void velocity_issue2(const VelMaps& ms, const VelMaps& mv, const ItemDesc* desc, int b,
+                                                int x0, int z0, float* st, uint64_t* bar, bool we) {
+    using G = TmaGeom<FP>;
+    const unsigned bytes = 4u * (G::WX * G::TZ + G::WX * G::WZ + G::TX * G::WZ + (we ? 5 : 4) * G::CEN) +
+                           (unsigned)sizeof(ItemDesc);
+    mbar_expect_tx(bar, bytes);
+    bulk_load(st + G::V_DESC, desc, (unsigned)sizeof(ItemDesc), bar);
+    tma_load_3d(st, &ms.sxx, x0 - G::HX, z0, b, bar);
+    tma_load_3d(st + G::HXO, &ms.szx, x0 - G::HX, z0 - FP, b, bar);
+    tma_load_3d(st + G::HXO + G::HXZ, &ms.szz, x0, z0 - FP, b, bar);
+    float* c = st + G::HXO + G::HXZ + G::HZO;
+    tma_load_2d(c, &mv.BX, x0, z0, bar);
+    tma_load_2d(c + G::CEN, &mv.BZ, x0, z0, bar);
+    tma_load_3d(c + 2 * G::CEN, &mv.vx, x0, z0, b, bar);
+    tma_load_3d(c + 3 * G::CEN, &mv.vz, x0, z0, b, bar);
+    if (we) tma_load_3d(c + 4 * G::CEN, &mv.We, x0, z0, b, bar);
+}
+
 template <int FP, bool INTERIOR>
 __device__ __forceinline__ void velocity_rows(const ItemDesc& D, const float* st, int x0, int z0, unsigned flags,
                                               const float2 (&hx)[FP], const float2 (&hz)[FP], long long msrc) {
@@ -1130,10 +1152,16 @@ __device__ __forceinline__ void staged_weights(const ItemDesc& D, float2 (&hx)[F
     }
 }
 
+// Launch arguments: mx = the maps of the buffer the state is read from, my =
+// of the buffer it is written to, items = the descriptors writing to my's
+// buffer, msrc = (source - destination) in floats for the CPML memories
+// (mx == my and msrc == 0 in place).
 template <int FP>
 __global__ void __launch_bounds__(kTmaThreads, 1)
-    stress_tma_multi_kernel(const MultiMaps* __restrict__ maps, const ItemDesc* __restrict__ items,
-                            const Tile* __restrict__ tiles, int ntiles, int it, unsigned flags, int* err) {
+    stress_tma_multi_kernel(const MultiMaps* __restrict__ mx, const MultiMaps* __restrict__ my,
+                            const ItemDesc* __restrict__ items, const Tile* __restrict__ tiles, int ntiles, int it,
+                            unsigned flags, long long msrc, int* err) {
+    const MultiMaps* maps = mx;
     using G = TmaGeom<FP>;
     tma_pipeline<FP, G::S_STAGE>(
         ntiles, err,
@@ -1150,14 +1178,17 @@ __global__ void __launch_bounds__(kTmaThreads, 1)
             const ItemDesc& D = *reinterpret_cast<const ItemDesc*>(st + G::S_DESC);
             float2 hx[FP], hz[FP];
             staged_weights<FP>(D, hx, hz);
-            stress_compute<FP>(D, model_ranges(D), st, c.y, c.z, it, flags, hx, hz);
+            TmaGrid gg = model_ranges(D);
+            gg.msrc = msrc;
+            stress_compute<FP>(D, gg, st, c.y, c.z, it, flags, hx, hz);
         });
 }
 
 template <int FP>
 __global__ void __launch_bounds__(kTmaThreads, 1)
-    velocity_tma_multi_kernel(const MultiMaps* __restrict__ maps, const ItemDesc* __restrict__ items,
-                              const Tile* __restrict__ tiles, int ntiles, int it, unsigned flags, int adj, int* err) {
+    velocity_tma_multi_kernel(const MultiMaps* __restrict__ mx, const MultiMaps* __restrict__ my,
+                              const ItemDesc* __restrict__ items, const Tile* __restrict__ tiles, int ntiles, int it,
+                              unsigned flags, int adj, long long msrc, int* err) {
     using G = TmaGeom<FP>;
     const bool we = (flags & FL_WE) != 0;
     tma_pipeline<FP, G::V_STAGE>(
@@ -1169,20 +1200,26 @@ __global__ void __launch_bounds__(kTmaThreads, 1)
             *z0 = T.z0;
         },
         [&](int b, int x0, int z0, float* st, uint64_t* bar) {
-            velocity_issue<FP>(adj ? maps[b].va : maps[b].vf, items + b, 0, x0, z0, st, bar, we);
+            if (adj) velocity_issue<FP>(mx[b].va, items + b, 0, x0, z0, st, bar, we);
+            else velocity_issue2<FP>(my[b].vf, mx[b].vf, items + b, 0, x0, z0, st, bar, we);
         },
         [&](int4 c, int4, const float* st) {
             const ItemDesc& D = *reinterpret_cast<const ItemDesc*>(st + G::V_DESC);
             float2 hx[FP], hz[FP];
             staged_weights<FP>(D, hx, hz);
-            velocity_compute<FP>(D, model_ranges(D), st, c.y, c.z, flags, hx, hz);
+            TmaGrid gg = model_ranges(D);
+            gg.msrc = msrc;
+            velocity_compute<FP>(D, gg, st, c.y, c.z, flags, hx, hz);
         });
 }
 
+// mx: the maps whose forward fields (AdjMaps::fv*) name the buffer holding
+// the forward state.
 template <int FP>
 __global__ void __launch_bounds__(kTmaThreads, 1)
-    adjoint_tma_multi_kernel(const MultiMaps* __restrict__ maps, const ItemDesc* __restrict__ items,
+    adjoint_tma_multi_kernel(const MultiMaps* __restrict__ mx, const ItemDesc* __restrict__ items,
                              const Tile* __restrict__ tiles, int ntiles, int it, unsigned flags, int* err) {
+    const MultiMaps* maps = mx;
     using G = AdjGeom<FP>;
     const bool grad = (flags & FL_GRAD) != 0;
     GradAhead none;
