@@ -34,11 +34,13 @@ namespace fwi {
 constexpr int kTmaTX = 128;      // tile columns
 constexpr int kTmaTZ = 16;       // tile rows
 constexpr int kTmaThreads = 512; // forward: a column pair and two rows each; adjoint: a column and two rows
-// stages in flight per CTA: three while they fit the 227 KB of shared memory
-// (half orders up to 4), two above
-template <int FP>
-__host__ __device__ constexpr int tma_stages() {
-    return FP <= 4 ? 3 : 2;
+// stages in flight per CTA for a stage of the given size: as many as fit the
+// 227 KB of shared memory (with the barriers), at most six -- three for the
+// forward passes up to half order 4 and for every adjoint pass, two for the
+// forward passes above
+template <int STAGE_FLOATS>
+__host__ __device__ constexpr int stages_for() {
+    return (232448 - 512) / (STAGE_FLOATS * 4) < 6 ? (232448 - 512) / (STAGE_FLOATS * 4) : 6;
 }
 constexpr unsigned long long kWaitNs = 2000000000ull;  // 2 s
 
@@ -675,7 +677,7 @@ __host__ __device__ constexpr size_t tma_tail_bytes() {
 
 template <int FP, int STAGE_FLOATS, class Coords, class Issue, class Compute>
 __device__ __forceinline__ void tma_pipeline(int ntiles, int* err, Coords coords, Issue issue, Compute compute) {
-    constexpr int kTmaStages = tma_stages<FP>();
+    constexpr int kTmaStages = stages_for<STAGE_FLOATS>();
     static_assert(STAGE_FLOATS % 32 == 0, "stages are 128-byte multiples");
     // dynamic shared memory only: the stages, the tile coordinates, the barriers
     extern __shared__ __align__(128) float tma_smem[];
@@ -741,11 +743,13 @@ __device__ __forceinline__ void tma_pipeline(int ntiles, int* err, Coords coords
 
 template <int FP>
 constexpr size_t stress_tma_smem() {
-    return sizeof(float) * tma_stages<FP>() * TmaGeom<FP>::S_STAGE + tma_tail_bytes<tma_stages<FP>()>();
+    constexpr int S = stages_for<TmaGeom<FP>::S_STAGE>();
+    return sizeof(float) * S * TmaGeom<FP>::S_STAGE + tma_tail_bytes<S>();
 }
 template <int FP>
 constexpr size_t velocity_tma_smem() {
-    return sizeof(float) * tma_stages<FP>() * TmaGeom<FP>::V_STAGE + tma_tail_bytes<tma_stages<FP>()>();
+    constexpr int S = stages_for<TmaGeom<FP>::V_STAGE>();
+    return sizeof(float) * S * TmaGeom<FP>::V_STAGE + tma_tail_bytes<S>();
 }
 static_assert(stress_tma_smem<4>() <= 232448 && velocity_tma_smem<4>() <= 232448, "shared memory per CTA");
 static_assert(stress_tma_smem<6>() <= 232448 && velocity_tma_smem<6>() <= 232448, "shared memory per CTA");
@@ -815,7 +819,8 @@ struct AdjMaps {
 
 template <int FP>
 __host__ __device__ constexpr size_t adjoint_tma_smem() {
-    return sizeof(float) * tma_stages<FP>() * AdjGeom<FP>::STAGE + tma_tail_bytes<tma_stages<FP>()>();
+    constexpr int S = stages_for<AdjGeom<FP>::STAGE>();
+    return sizeof(float) * S * AdjGeom<FP>::STAGE + tma_tail_bytes<S>();
 }
 static_assert(adjoint_tma_smem<4>() <= 232448 && adjoint_tma_smem<6>() <= 232448, "shared memory per CTA");
 
