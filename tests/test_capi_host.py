@@ -132,3 +132,33 @@ def test_checkpoint_plan_large():
     assert adj == list(range(2999, -1, -1))
     # Griewank-Walther bound with S = 33 stored states: r*n - beta(S+1, r-1), r = 3
     assert cost == 3 * 3000 - 595 - 35
+
+
+@pytest.mark.parametrize("n,s", [(10, 2), (120, 5), (150, 3), (75, 40), (3000, 32)])
+def test_plan_restatement_matches_library(n, s):
+    """tests/_plan.py (used to check the recompute count the engines report)
+    restates the library's planner: same actions in the same order, and the
+    forward steps left after the first sweep's checkpoints."""
+    import _plan
+    kinds = {0: "A", 1: "S", 2: "R", 3: "J"}
+    plan, cost = _capi.checkpoint_plan(n, s)
+    mine = _plan.plan(n, s)
+    assert len(mine) == len(plan)
+    for (k, a, b), m in zip(plan, mine):
+        assert kinds[k] == m[0]
+        if k == 0:
+            assert (a, b) == (m[1], m[2])
+        elif k in (1, 2):
+            assert (a, b) == (m[1], m[2])
+        else:
+            assert a == m[1]
+    assert sum(m[2] - m[1] for m in mine if m[0] == "A") == cost
+    # the count after the prefix: re-derived here from the library's actions
+    k = 0
+    last = 0
+    while plan[k][0] != 3:
+        if plan[k][0] == 1:
+            last = plan[k][2]
+        k += 1
+    want = (n - 1 - last) + sum(b - a for (kind, a, b) in plan[k:] if kind == 0)
+    assert _plan.recompute_after_first_sweep(n, s) == want
