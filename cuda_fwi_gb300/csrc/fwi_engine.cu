@@ -1046,11 +1046,13 @@ struct Engine {
             rb_valid = true;
         }
         if (keep && ckpt_mode() && want_slots > 0) {
+            const size_t before = d_snap.bytes;  // ensure() only ever reallocates larger
             FWI_TRY(grow(d_snap, (size_t)want_slots * cap * state * 4));
             // the copy-free plan steps into any checkpoint buffer: cells that no
-            // pass writes (grid borders) must read as zero there too
-            if (kmap == 3 && !exact())
-                CUDA_TRY(cudaMemsetAsync(d_snap.p, 0, (size_t)want_slots * nb * state * 4, stream));
+            // pass writes (grid borders) must read as zero there too.  Fresh
+            // memory is zeroed once; everything written into it later is a
+            // whole state, whose border cells are zero.
+            if (d_snap.bytes != before) CUDA_TRY(cudaMemsetAsync(d_snap.p, 0, d_snap.bytes, stream));
         }
         if (exact()) {
             FWI_TRY(grow(d_nxt, (size_t)cap * state * 4));
