@@ -352,6 +352,27 @@ def main():
                  "how": f"{args.plain_shots} shot(s), one shot per launch, direct launches (no graph), "
                         f"same kernels and binomial checkpointing; host wall clock"}
         pe.close()
+        # context: the same one-shot path on the scalar one-thread-per-cell kernels
+        # (the reference's GPU kernel design), and the bound the roofline puts on
+        # any batched path: algorithmic bytes per shot-gradient / measured HBM peak
+        pc = Engine(syn, device=local)
+        pc.set_exec(False, 32, 0, 1)
+        pc.set_strategy("binomial", snapshots=args.snapshots)
+        pc.gradient([0], obs)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        pc.gradient([0], obs)
+        torch.cuda.synchronize()
+        pcs = time.perf_counter() - t0
+        pc.close()
+        fb = [x / sub for x in algorithmic_bytes(syn, sub)]  # per shot, materials shared by a launch
+        per_grad = (syn.nt + recompute) * (fb[0] + fb[1]) + syn.nt * (fb[2] + fb[3]) + \
+            syn.nt * (syn.nxt - 2 * syn.fpad) * (syn.nzt - 2 * syn.fpad) * 8  # + energy of the recording sweep
+        bound = peak * 1e9 / per_grad
+        plain.update({"scalar_cells_shot_gradients_s": 1.0 / pcs,
+                      "batched_over_plain_scalar_cells": (value / world) * pcs,
+                      "roofline_bound_shot_gradients_s": bound,
+                      "roofline_bound_over_plain": bound * ps})
 
     # ---- the other strategy of the workload: random-boundary reconstruction ----
     rbinfo = None
