@@ -127,6 +127,7 @@ def test_exact_gradient_central_fd_config2_reduced():
     obs = O.forward(t, 0)["rec"]
     for name, (got, fd) in _fd_check(p, obs, 32, seed=11).items():
         # relative L2 over the 32 cells; the FD step's own error is ~1e-6
+        print(f"config 2 reduced, {name}: rel L2 vs central FD {rel_l2(got, fd):.2e}")
         assert rel_l2(got, fd) <= 1e-4, name
 
 
@@ -137,4 +138,5 @@ def test_exact_gradient_central_fd_config2_full():
     p = P.config2(True, seed=7)
     obs = O.forward(t, 0)["rec"]
     for name, (got, fd) in _fd_check(p, obs, 32, seed=11).items():
+        print(f"config 2 full size, {name}: rel L2 vs central FD {rel_l2(got, fd):.2e}")
         assert rel_l2(got, fd) <= 1e-4, name
