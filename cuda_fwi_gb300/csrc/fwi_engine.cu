@@ -352,17 +352,17 @@ struct TmaSet {
 template <int FP>
 static void t_stress(dim3 g, cudaStream_t s, const StressMaps& m, const ItemDesc* it, TmaGrid tg, int step,
                      unsigned flags, int* err) {
-    stress_tma_kernel<FP><<<g, kTmaThreads, stress_tma_smem<FP>(), s>>>(m, it, tg, step, flags, err);
+    stress_tma_kernel<FP><<<g, kFwdThreads, stress_tma_smem<FP>(), s>>>(m, it, tg, step, flags, err);
 }
 template <int FP>
 static void t_velocity(dim3 g, cudaStream_t s, const VelMaps& m, const ItemDesc* it, TmaGrid tg, int step,
                        unsigned flags, int* err) {
-    velocity_tma_kernel<FP><<<g, kTmaThreads, velocity_tma_smem<FP>(), s>>>(m, it, tg, step, flags, err);
+    velocity_tma_kernel<FP><<<g, kFwdThreads, velocity_tma_smem<FP>(), s>>>(m, it, tg, step, flags, err);
 }
 template <int FP>
 static void t_adjoint(dim3 g, cudaStream_t s, const AdjMaps& m, const ItemDesc* it, TmaGrid tg, int step,
                       unsigned flags, int* err) {
-    adjoint_tma_kernel<FP><<<g, kTmaThreads, adjoint_tma_smem<FP>(), s>>>(m, it, tg, step, flags, err);
+    adjoint_tma_kernel<FP><<<g, kAdjThreads, adjoint_tma_smem<FP>(), s>>>(m, it, tg, step, flags, err);
 }
 template <int FP>
 static cudaError_t t_prepare() {
@@ -424,19 +424,19 @@ struct TmaMultiSet {
 template <int FP>
 static void tm_stress(dim3 g, cudaStream_t s, const MultiMaps* mx, const MultiMaps* my, const ItemDesc* it,
                       const Tile* t, int nt, int step, unsigned flags, int, long long msrc, int* err) {
-    stress_tma_multi_kernel<FP><<<g, kTmaThreads, stress_tma_smem<FP>(), s>>>(mx, my, it, t, nt, step, flags, msrc,
+    stress_tma_multi_kernel<FP><<<g, kFwdThreads, stress_tma_smem<FP>(), s>>>(mx, my, it, t, nt, step, flags, msrc,
                                                                                  err);
 }
 template <int FP>
 static void tm_velocity(dim3 g, cudaStream_t s, const MultiMaps* mx, const MultiMaps* my, const ItemDesc* it,
                         const Tile* t, int nt, int step, unsigned flags, int adj, long long msrc, int* err) {
-    velocity_tma_multi_kernel<FP><<<g, kTmaThreads, velocity_tma_smem<FP>(), s>>>(mx, my, it, t, nt, step, flags,
+    velocity_tma_multi_kernel<FP><<<g, kFwdThreads, velocity_tma_smem<FP>(), s>>>(mx, my, it, t, nt, step, flags,
                                                                                      adj, msrc, err);
 }
 template <int FP>
 static void tm_adjoint(dim3 g, cudaStream_t s, const MultiMaps* mx, const MultiMaps*, const ItemDesc* it,
                        const Tile* t, int nt, int step, unsigned flags, int, long long, int* err) {
-    adjoint_tma_multi_kernel<FP><<<g, kTmaThreads, adjoint_tma_smem<FP>(), s>>>(mx, it, t, nt, step, flags, err);
+    adjoint_tma_multi_kernel<FP><<<g, kAdjThreads, adjoint_tma_smem<FP>(), s>>>(mx, it, t, nt, step, flags, err);
 }
 template <int FP>
 static cudaError_t tm_prepare() {

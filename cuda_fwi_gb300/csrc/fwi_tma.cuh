@@ -31,9 +31,18 @@
 
 namespace fwi {
 
-constexpr int kTmaTX = 128;      // tile columns
-constexpr int kTmaTZ = 16;       // tile rows
-constexpr int kTmaThreads = 512; // forward: a column pair and two rows each; adjoint: a column and two rows
+// Forward tile rows (a variant build may set 20 or 24: 640 or 768 threads, two
+// stages, 96 or 80 registers with spills; on 32 shots of the 1068x568 grid,
+// order 8, they ran at 0.159 / 0.192 ms per stress launch against 0.143 for 16).
+#ifndef FWI_TMA_ROWS
+#define FWI_TMA_ROWS 16
+#endif
+constexpr int kTmaTX = 128;           // tile columns
+constexpr int kTmaTZ = FWI_TMA_ROWS;  // forward tile rows
+constexpr int kPairRows = 2;          // forward: a thread owns a column pair of two rows
+constexpr int kFwdThreads = (kTmaTX / 2) * (kTmaTZ / kPairRows);
+constexpr int kAdjThreads = 512;      // adjoint: a thread owns a column pair of one row (128 x 8 tiles)
+static_assert(kTmaTZ % kPairRows == 0 && kFwdThreads <= 1024, "forward tile rows");
 // stages in flight per CTA for a stage of the given size: as many as fit the
 // 227 KB of shared memory (with the barriers), at most six -- three for the
 // forward passes up to half order 4 and for every adjoint pass, two for the
@@ -167,8 +176,6 @@ __device__ __forceinline__ void tile_coords(const TmaGrid& g, int t, int* b, int
 // is one FP32x2 instruction for both columns (each lane rounded like the
 // scalar operation), which halves the load and arithmetic instructions per
 // cell of the one-column mapping.
-constexpr int kPairRows = 2;  // rows per thread (64 column pairs x 8 row groups = 128 x 16)
-static_assert((kTmaTX / 2) * (kTmaTZ / kPairRows) == kTmaThreads, "one thread per column pair and row pair");
 static_assert(kTmaTX == 128 && kPairRows == 2, "a warp covers 64 columns of one row pair");
 
 __device__ __forceinline__ float2 bc2(float a) { return make_float2(a, a); }
@@ -755,7 +762,7 @@ static_assert(stress_tma_smem<4>() <= 232448 && velocity_tma_smem<4>() <= 232448
 static_assert(stress_tma_smem<6>() <= 232448 && velocity_tma_smem<6>() <= 232448, "shared memory per CTA");
 
 template <int FP>
-__global__ void __launch_bounds__(kTmaThreads, 1)
+__global__ void __launch_bounds__(kFwdThreads, 1)
     stress_tma_kernel(const __grid_constant__ StressMaps maps, const ItemDesc* __restrict__ items,
                       const TmaGrid g, int it, unsigned flags, int* err) {
     using G = TmaGeom<FP>;
@@ -773,7 +780,7 @@ __global__ void __launch_bounds__(kTmaThreads, 1)
 }
 
 template <int FP>
-__global__ void __launch_bounds__(kTmaThreads, 1)
+__global__ void __launch_bounds__(kFwdThreads, 1)
     velocity_tma_kernel(const __grid_constant__ VelMaps maps, const ItemDesc* __restrict__ items,
                         const TmaGrid g, int it, unsigned flags, int* err) {
     using G = TmaGeom<FP>;
@@ -853,7 +860,7 @@ __device__ __forceinline__ void adjoint_issue(const AdjMaps& m, const ItemDesc* 
 
 // The adjoint pass maps a column pair to each thread and one tile row
 // (64 pairs x 8 rows); warp w covers 64 columns of tile row w / 2.
-static_assert((kTmaTX / 2) * kAdjTZ == kTmaThreads, "one thread per column pair of a row");
+static_assert((kTmaTX / 2) * kAdjTZ == kAdjThreads, "one thread per column pair of a row");
 
 // The warp's cells are plain-stencil cells and, on a gradient step, lie in
 // the gradient window sampled at unit intervals.
@@ -1061,7 +1068,7 @@ __device__ __forceinline__ void adjoint_rows(const ItemDesc& D, const float* st,
 }
 
 template <int FP>
-__global__ void __launch_bounds__(kTmaThreads, 1)
+__global__ void __launch_bounds__(kAdjThreads, 1)
     adjoint_tma_kernel(const __grid_constant__ AdjMaps maps, const ItemDesc* __restrict__ items, const TmaGrid g,
                        int it, unsigned flags, int* err) {
     using G = AdjGeom<FP>;
@@ -1162,7 +1169,7 @@ __device__ __forceinline__ void staged_weights(const ItemDesc& D, float2 (&hx)[F
 // buffer, msrc = (source - destination) in floats for the CPML memories
 // (mx == my and msrc == 0 in place).
 template <int FP>
-__global__ void __launch_bounds__(kTmaThreads, 1)
+__global__ void __launch_bounds__(kFwdThreads, 1)
     stress_tma_multi_kernel(const MultiMaps* __restrict__ mx, const MultiMaps* __restrict__ my,
                             const ItemDesc* __restrict__ items, const Tile* __restrict__ tiles, int ntiles, int it,
                             unsigned flags, long long msrc, int* err) {
@@ -1190,7 +1197,7 @@ __global__ void __launch_bounds__(kTmaThreads, 1)
 }
 
 template <int FP>
-__global__ void __launch_bounds__(kTmaThreads, 1)
+__global__ void __launch_bounds__(kFwdThreads, 1)
     velocity_tma_multi_kernel(const MultiMaps* __restrict__ mx, const MultiMaps* __restrict__ my,
                               const ItemDesc* __restrict__ items, const Tile* __restrict__ tiles, int ntiles, int it,
                               unsigned flags, int adj, long long msrc, int* err) {
@@ -1221,7 +1228,7 @@ __global__ void __launch_bounds__(kTmaThreads, 1)
 // mx: the maps whose forward fields (AdjMaps::fv*) name the buffer holding
 // the forward state.
 template <int FP>
-__global__ void __launch_bounds__(kTmaThreads, 1)
+__global__ void __launch_bounds__(kAdjThreads, 1)
     adjoint_tma_multi_kernel(const MultiMaps* __restrict__ mx, const ItemDesc* __restrict__ items,
                              const Tile* __restrict__ tiles, int ntiles, int it, unsigned flags, int* err) {
     const MultiMaps* maps = mx;
