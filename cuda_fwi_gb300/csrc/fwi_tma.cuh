@@ -276,28 +276,44 @@ __device__ __forceinline__ PairCols pair_cols(const ItemDesc& D, int ix, bool st
     return pc;
 }
 
-// CPML of an x-derivative pair (d1 with the integer-grid coefficients, d2 with
-// the half-grid ones): memories m1/m2 of each lane in an x-strip are advanced
-// and stored, and the lane's derivatives corrected.  The coefficients are
-// re-read per row (L1 hits) rather than held in registers by every thread.
+// CPML of lane l of an x-derivative pair inside an x-strip (d1 with the
+// integer-grid coefficients, d2 with the half-grid ones): its memories m1/m2
+// at m are advanced from o1/o2 and stored, and its derivatives corrected.
+__device__ __forceinline__ void cpml_x_lane(const Cpml& c, size_t m, float o1, float o2, float* __restrict__ a1,
+                                            float* __restrict__ a2, float& e1, float& e2) {
+    const float m1 = c.b * o1 + c.a * e1;
+    const float m2 = c.bh * o2 + c.ah * e2;
+    a1[m] = m1;
+    a2[m] = m2;
+    e1 = e1 * c.iK + m1;
+    e2 = e2 * c.iKh + m2;
+}
+// Both lanes of a pair, each lane's coefficients read at the row (L1 hits):
+// the stress and adjoint passes, where holding them across rows costs spills.
 __device__ __forceinline__ void cpml_x_pair(const PairCols& pc, const float* __restrict__ cpml, int iz, int tp,
                                             const float (&o1)[2], const float (&o2)[2], float* __restrict__ a1,
                                             float* __restrict__ a2, float2& d1, float2& d2) {
 #pragma unroll
-    for (int l = 0; l < 2; l++) {
-        if (pc.px[l] >= 0) {
-            const Cpml c = load_cpml(cpml, tp, pc.px[l]);
-            float& e1 = l ? d1.y : d1.x;
-            float& e2 = l ? d2.y : d2.x;
-            const size_t m = (size_t)iz * tp + pc.px[l];
-            const float m1 = c.b * o1[l] + c.a * e1;
-            const float m2 = c.bh * o2[l] + c.ah * e2;
-            a1[m] = m1;
-            a2[m] = m2;
-            e1 = e1 * c.iK + m1;
-            e2 = e2 * c.iKh + m2;
-        }
-    }
+    for (int l = 0; l < 2; l++)
+        if (pc.px[l] >= 0)
+            cpml_x_lane(load_cpml(cpml, tp, pc.px[l]), (size_t)iz * tp + pc.px[l], o1[l], o2[l], a1, a2,
+                        l ? d1.y : d1.x, l ? d2.y : d2.x);
+}
+// Both lanes with coefficients cx[l] read once per tile (load_cpml_x): the
+// velocity pass up to half order 4, whose two rows share them.
+__device__ __forceinline__ void load_cpml_x(const PairCols& pc, const float* __restrict__ cpml, int tp,
+                                            Cpml (&cx)[2]) {
+#pragma unroll
+    for (int l = 0; l < 2; l++)
+        if (pc.px[l] >= 0) cx[l] = load_cpml(cpml, tp, pc.px[l]);
+}
+__device__ __forceinline__ void cpml_x_pair(const PairCols& pc, const Cpml (&cx)[2], int iz, int tp,
+                                            const float (&o1)[2], const float (&o2)[2], float* __restrict__ a1,
+                                            float* __restrict__ a2, float2& d1, float2& d2) {
+#pragma unroll
+    for (int l = 0; l < 2; l++)
+        if (pc.px[l] >= 0)
+            cpml_x_lane(cx[l], (size_t)iz * tp + pc.px[l], o1[l], o2[l], a1, a2, l ? d1.y : d1.x, l ? d2.y : d2.x);
 }
 
 // z-strip index of row iz (-1 outside the strips); the stress pass's top strip
@@ -576,7 +592,12 @@ __device__ __forceinline__ void velocity_rows(const ItemDesc& D, const float* st
     float mx1[R][2], mx2[R][2];
     float2 mz1[R], mz2[R];
     int pzr[R];
+    // x-strip coefficients read once per tile up to half order 4 (both rows use
+    // them); above, per row, as held across the rows they cost spills
+    constexpr bool kHoistCx = FP <= 4;
+    Cpml cx[2];
     if constexpr (!INTERIOR) {
+        if constexpr (kHoistCx) load_cpml_x(pc, D.cpml, tp, cx);
 #pragma unroll
         for (int rr = 0; rr < R; rr++) {
             const int iz = z0 + r0 + rr;
@@ -619,7 +640,8 @@ __device__ __forceinline__ void velocity_rows(const ItemDesc& D, const float* st
             szz_z = fma2(hz[k - 1], sub2(wsz[rr + k + FP - 1], wsz[rr - k + FP]), szz_z);
         }
         if constexpr (!INTERIOR) {
-            cpml_x_pair(pc, D.cpml, iz, tp, mx1[rr], mx2[rr], msxx_x, mszx_x, sxx_x, szx_x);
+            if constexpr (kHoistCx) cpml_x_pair(pc, cx, iz, tp, mx1[rr], mx2[rr], msxx_x, mszx_x, sxx_x, szx_x);
+            else cpml_x_pair(pc, D.cpml, iz, tp, mx1[rr], mx2[rr], msxx_x, mszx_x, sxx_x, szx_x);
             if (pzr[rr] >= 0) {
                 const Cpml cz = load_cpml(D.cpml, tp, pzr[rr]);
                 const size_t m = (size_t)pzr[rr] * P + ix;
