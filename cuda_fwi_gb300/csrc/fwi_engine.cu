@@ -620,7 +620,7 @@ struct Engine {
     // geometry / scheme
     int nt, nzt, nxt, fpad, ppad, npml, fsurf, fdorder, tp, pitch, pnx, pnz;
     double dt, dx, dz, hc[7];
-    std::vector<float> cpml_h;  // [6][tp]
+    std::vector<float> cpml_h;  // [6][tp], then the same per column: [tp][6]
     // FWI window
     int fwi_dt = 1, fwi_dx = 1, fwi_dz = 1, wx1 = 0, wx2 = 0, wz1 = 0, wz2 = 0;
     int nft = 0, nfz = 0, nfx = 0;
@@ -726,7 +726,7 @@ struct Engine {
         // bottom CPML offset: the reference's for fdorder 2; with a free surface at
         // higher orders the offset keeps the layer on indices npml+1..2npml+1
         pnz = fsurf ? nzt - 2 * ppad + fpad - 2 : nzt - 2 * ppad + fpad - 1;
-        cpml_h.assign(6 * (size_t)tp, 0.f);
+        cpml_h.assign(12 * (size_t)tp, 0.f);
         if (npml > 0) {
             if (!d->a || !d->b || !d->K || !d->a_half || !d->b_half || !d->K_half)
                 return fail(FWI_ERR_INVALID, "CPML profiles are required when npml > 0");
@@ -745,6 +745,7 @@ struct Engine {
                 cpml_h[4 * tp + i] = (float)d->b_half[i];
                 cpml_h[5 * tp + i] = (float)(1.0 / d->K_half[i]);
             }
+            interleave_cpml(cpml_h.data(), tp);
         }
         field = (size_t)nzt * pitch;
         xstrip = round_up((size_t)nzt * tp, 32);

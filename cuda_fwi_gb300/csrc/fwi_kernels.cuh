@@ -100,6 +100,26 @@ __device__ __forceinline__ Cpml load_cpml(const float* __restrict__ c, int tp, i
     return r;
 }
 
+// The engines store a grid's coefficient table as [6][tp] (a, b, 1/K, a_half,
+// b_half, 1/K_half per strip index) followed by the same values per index,
+// [tp][6]: the TMA-staged kernels read one index with three 8-byte loads.
+inline void interleave_cpml(float* t, int tp) {
+    for (int i = 0; i < tp; i++)
+        for (int k = 0; k < 6; k++) t[6 * tp + 6 * i + k] = t[k * tp + i];
+}
+__device__ __forceinline__ Cpml load_cpml6(const float* __restrict__ c, int tp, int p) {
+    const float2* q = reinterpret_cast<const float2*>(c + 6 * tp) + 3 * p;
+    const float2 u = __ldg(q), v = __ldg(q + 1), w = __ldg(q + 2);
+    Cpml r;
+    r.a = u.x;
+    r.b = u.y;
+    r.iK = v.x;
+    r.ah = v.y;
+    r.bh = w.x;
+    r.iKh = w.y;
+    return r;
+}
+
 // Stress pass over one tile (forward or adjoint; the reference uses the same
 // operator for both).  One thread per column marches down the rows.  All
 // descriptor fields are copied into registers first; the per-row loads that

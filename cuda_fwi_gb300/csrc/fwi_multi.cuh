@@ -142,7 +142,7 @@ struct MultiEngine {
             I.off_mat = total_mat;
             total_mat += 5 * I.field;
             I.off_cpml = total_cpml;
-            total_cpml += round_up(6 * (size_t)I.tp, 32);
+            total_cpml += round_up(12 * (size_t)I.tp, 32);
             I.off_grad = total_grad;
             total_grad += round_up(3 * (size_t)I.nfz * I.nfx, 32);
             I.nsrc = m[b].nsrc;
@@ -161,7 +161,7 @@ struct MultiEngine {
                     m[b].rec_z[i] >= I.nzt - I.fpad)
                     return fail(FWI_ERR_INVALID, tag + "receiver outside the interior");
             // CPML profile (index npml must be the identity, as for the single-model engine)
-            std::vector<float> cp(round_up(6 * (size_t)I.tp, 32), 0.f);
+            std::vector<float> cp(round_up(12 * (size_t)I.tp, 32), 0.f);
             if (I.npml > 0) {
                 if (!d.a || !d.b || !d.K || !d.a_half || !d.b_half || !d.K_half)
                     return fail(FWI_ERR_INVALID, tag + "CPML profiles are required when npml > 0");
@@ -175,6 +175,7 @@ struct MultiEngine {
                     cp[4 * I.tp + i] = (float)d.b_half[i];
                     cp[5 * I.tp + i] = (float)(1.0 / d.K_half[i]);
                 }
+                interleave_cpml(cp.data(), I.tp);
             }
             cpml_h.insert(cpml_h.end(), cp.begin(), cp.end());
             // materials, dt-scaled (the same FP64 averages as fwi_psv_set_model_lmr)

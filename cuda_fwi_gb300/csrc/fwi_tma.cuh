@@ -296,7 +296,7 @@ __device__ __forceinline__ void cpml_x_pair(const PairCols& pc, const float* __r
 #pragma unroll
     for (int l = 0; l < 2; l++)
         if (pc.px[l] >= 0)
-            cpml_x_lane(load_cpml(cpml, tp, pc.px[l]), (size_t)iz * tp + pc.px[l], o1[l], o2[l], a1, a2,
+            cpml_x_lane(load_cpml6(cpml, tp, pc.px[l]), (size_t)iz * tp + pc.px[l], o1[l], o2[l], a1, a2,
                         l ? d1.y : d1.x, l ? d2.y : d2.x);
 }
 // Both lanes with coefficients cx[l] read once per tile (load_cpml_x): the
@@ -305,7 +305,7 @@ __device__ __forceinline__ void load_cpml_x(const PairCols& pc, const float* __r
                                             Cpml (&cx)[2]) {
 #pragma unroll
     for (int l = 0; l < 2; l++)
-        if (pc.px[l] >= 0) cx[l] = load_cpml(cpml, tp, pc.px[l]);
+        if (pc.px[l] >= 0) cx[l] = load_cpml6(cpml, tp, pc.px[l]);
 }
 __device__ __forceinline__ void cpml_x_pair(const PairCols& pc, const Cpml (&cx)[2], int iz, int tp,
                                             const float (&o1)[2], const float (&o2)[2], float* __restrict__ a1,
@@ -447,7 +447,7 @@ __device__ __forceinline__ void stress_rows(const ItemDesc& D, const float* st, 
         if constexpr (!INTERIOR) {
             cpml_x_pair(pc, D.cpml, iz, tp, mx1[rr], mx2[rr], mvx_x, mvz_x, vx_x, vz_x);
             if (pzr[rr] >= 0) {
-                const Cpml cz = load_cpml(D.cpml, tp, pzr[rr]);
+                const Cpml cz = load_cpml6(D.cpml, tp, pzr[rr]);
                 const size_t m = (size_t)pzr[rr] * P + ix;
                 const float2 m1 = fma2(bc2(cz.b), mz1[rr], mul2(bc2(cz.a), vz_z));
                 const float2 m2 = fma2(bc2(cz.bh), mz2[rr], mul2(bc2(cz.ah), vx_z));
@@ -643,7 +643,7 @@ __device__ __forceinline__ void velocity_rows(const ItemDesc& D, const float* st
             if constexpr (kHoistCx) cpml_x_pair(pc, cx, iz, tp, mx1[rr], mx2[rr], msxx_x, mszx_x, sxx_x, szx_x);
             else cpml_x_pair(pc, D.cpml, iz, tp, mx1[rr], mx2[rr], msxx_x, mszx_x, sxx_x, szx_x);
             if (pzr[rr] >= 0) {
-                const Cpml cz = load_cpml(D.cpml, tp, pzr[rr]);
+                const Cpml cz = load_cpml6(D.cpml, tp, pzr[rr]);
                 const size_t m = (size_t)pzr[rr] * P + ix;
                 const float2 m1 = fma2(bc2(cz.b), mz1[rr], mul2(bc2(cz.a), szz_z));
                 const float2 m2 = fma2(bc2(cz.bh), mz2[rr], mul2(bc2(cz.ah), szx_z));
@@ -1013,7 +1013,7 @@ __device__ __forceinline__ void adjoint_rows(const ItemDesc& D, const float* st,
     if constexpr (!INTERIOR) {
         cpml_x_pair(pc, D.cpml, iz, tp, mx1, mx2, D.mvx_x, D.mvz_x, vx_x, vz_x);
         if (pz >= 0) {
-            const Cpml cz = load_cpml(D.cpml, tp, pz);
+            const Cpml cz = load_cpml6(D.cpml, tp, pz);
             const size_t m = (size_t)pz * P + ix;
             const float2 m1 = fma2(bc2(cz.b), mz1, mul2(bc2(cz.a), vz_z));
             const float2 m2 = fma2(bc2(cz.bh), mz2, mul2(bc2(cz.ah), vx_z));
