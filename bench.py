@@ -41,6 +41,10 @@ HBM_FALLBACK_GBS = 6800.0
 
 
 def parse():
+    return parse_args(None)
+
+
+def parse_args(argv):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)
@@ -61,7 +65,7 @@ def parse():
     ap.add_argument("--block-x", type=int, default=0,
                     help="stencil thread mapping (set_exec block_x; 0 = engine default)")
     ap.add_argument("--no-cpu", action="store_true")
-    return ap.parse_args()
+    return ap.parse_args(argv)
 
 
 def peaks():
@@ -73,8 +77,11 @@ def peaks():
         return HBM_FALLBACK_GBS, "fallback"
 
 
-def workload(args):
+def workload(args, setup=None):
+    """(true, synthetic) problems of the workload; `setup` replaces the engine
+    library's setup helpers (the reference arm passes the oracle's)."""
     from cuda_fwi_gb300 import problem as P
+    P.use_setup_helpers(setup)
     true = P.config3(True, nshots=args.shots)
     syn = P.config3(False, nshots=args.shots)
     if args.nt:
@@ -92,6 +99,16 @@ def workload(args):
 WORKLOAD_DESC = ("1000x500 (1068x568 padded) elastic P-SV, dx=dz=10 m, dt=1 ms, nt=3000, "
                  "8th-order Holberg, 30-cell CPML, faulted layered model, 64 shots x 250 receivers, "
                  "binomial checkpointing 32 slots/shot, gradients summed over shots")
+
+
+def bench_config(args, syn, world):
+    """The workload's description, printed identically by both arms."""
+    return {"workload": WORKLOAD_DESC, "shots_per_step": args.shots, "nt": syn.nt,
+            "padded_grid": [syn.nzt, syn.nxt], "fdorder": syn.fdorder,
+            "checkpoints_per_shot": args.snapshots,
+            "l2": "inputs larger than L2 (per-step working set ~30 GB: 64 shot states, "
+                  "checkpoints, 192 MB observed data)",
+            "parallelism": f"replicas x{world}, shots batched in one launch per time step"}
 
 
 class ClockSampler:
@@ -157,11 +174,23 @@ def cpu_baseline(syn, args, nproc=None):
             "per_core_value": 1.0 / (r["per_process_s"] * syn.nt / r["nt_sample"])}
 
 
+def product_library_mapped():
+    """Whether this process has the engine library mapped (Linux /proc)."""
+    try:
+        with open("/proc/self/maps") as f:
+            return "libfwi_psv.so" in f.read()
+    except OSError:
+        return None
+
+
 def run_reference(args, rank):
     if rank != 0:
         return
     t0 = time.perf_counter()
-    _, syn = workload(args)
+    # the reference arm never loads the engine library: its problem is set up
+    # by the oracle's own helpers (bit-identical to the engine's host code)
+    from oracle import oracle as O
+    _, syn = workload(args, setup=O.setup_helpers)
     vals = []
     last = None
     for i in range(args.warmup + args.steps):
@@ -173,8 +202,9 @@ def run_reference(args, rank):
     out = {"impl": "reference", "metric": "shot-gradients/s", "value": v, "unit": "shot-gradients/s",
            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-           "data": "synthetic", "config": {"workload": WORKLOAD_DESC},
+           "data": "synthetic", "config": bench_config(args, syn, args.gpus),
            "cpu_baseline": last,
+           "product_library_mapped": product_library_mapped(),
            "e2e": {"value": v, "unit": "shot-gradients/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
            "wall_s": time.perf_counter() - t0}
     print(json.dumps(out), flush=True)
@@ -457,12 +487,8 @@ def main():
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": dev_s / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": WORKLOAD_DESC, "shots_per_step": B, "shots_per_launch": sub, "nt": syn.nt,
-                       "padded_grid": [syn.nzt, syn.nxt], "fdorder": syn.fdorder,
-                       "checkpoints_per_shot": args.snapshots,
-                       "l2": "inputs larger than L2 (per-step working set ~30 GB: 64 shot states, "
-                             "checkpoints, 192 MB observed data)",
-                       "parallelism": f"replicas x{world}, shots batched in one launch per time step"},
+            "config": bench_config(args, syn, world),
+            "shots_per_launch": sub,
             "gcell_upd_s": gcell,
             "gcell_upd_s_useful": gcell_useful,
             "time_steps_per_shot_gradient": steps_per_batch,

@@ -1,24 +1,40 @@
 """torch.autograd wrapper: the L2 waveform misfit of a batch of shots as a
 differentiable function of lam, mu, rho.
 
-    J = FWIMisfit.apply(lam, mu, rho, engine, shots, obs)
+    J = FWIMisfit.apply(lam, mu, rho, engine, shots, obs, "exact")
     J.backward()   # lam.grad, mu.grad, rho.grad
 
-forward returns sum over shots of J_s = sum 0.5 dt (syn - obs)^2 (the
-reference's calculate_l2_adjoint_sources, CUDA_week2/fd_wave_model.cu:972-1002);
-backward returns the gradient the engine computes -- the reference's
-correlation formula (adjoint_kernel_PSV_GPU.cu:830-863) by default, or the
-exact discrete adjoint after engine.set_gradient_mode("exact") -- placed on
-the FWI window cells of the padded grid (zero elsewhere).  The forward and the
-adjoint run together on the GPU in one fwi_psv_gradient call; backward only
-scales the stored gradient.
+``forward`` is the engine's forward entry point (``fwi_psv_forward``): it runs
+the shots' forward sweep, records their seismograms and returns
+J = sum over shots of sum 0.5 dt (syn - obs)^2 (the reference's
+calculate_l2_adjoint_sources, CUDA_week2/fd_wave_model.cu:972-1002), keeping
+what the backward needs (checkpoints or storage, the residual) on the device.
+``backward`` is the engine's backward entry point (``fwi_psv_backward``): the
+adjoint sweep and the gradient accumulation, summed over the shots and scaled
+by the incoming gradient.  A forward whose result never reaches ``backward``
+costs one forward sweep only.
 
-Tensors are CPU float64 [nzt][nxt] (the reference's host layout).
+The gradient mode is explicit:
+
+* ``"exact"`` (default) -- the discrete adjoint of the FP32 time stepping:
+  dJ/d(lam, mu, rho) of the very misfit ``forward`` returns, with respect to
+  the raw models (the staggered averages are differentiated too);
+* ``"reference"`` -- the reference's correlation formula
+  (adjoint_kernel_PSV_GPU.cu:830-863).  It is what the reference's FWI loop
+  uses, but it is not the derivative of J; choose it only to reproduce the
+  reference.
+
+Gradients are placed on the FWI window cells of the padded grid (zero
+elsewhere).  Tensors are CPU float64 [nzt][nxt] (the reference's host layout).
+Each forward must be followed by its backward before the engine runs another
+forward (the engine keeps one forward's state).
 """
 from __future__ import annotations
 
 import numpy as np
 import torch
+
+MODES = ("exact", "reference")
 
 
 def _to_grid(g, p):
@@ -32,19 +48,23 @@ def _to_grid(g, p):
 
 class FWIMisfit(torch.autograd.Function):
     @staticmethod
-    def forward(ctx, lam, mu, rho, engine, shots, obs):
+    def forward(ctx, lam, mu, rho, engine, shots, obs, mode="exact"):
+        if mode not in MODES:
+            raise ValueError(f"mode must be one of {MODES}, not {mode!r}")
+        engine.set_gradient_mode(mode)
         engine.set_model_lmr(lam.detach().cpu().numpy(), mu.detach().cpu().numpy(),
                              rho.detach().cpu().numpy())
-        g, mis = engine.gradient(list(shots), obs)
-        p = engine.p
-        ctx.grads = [torch.from_numpy(_to_grid(x, p)) for x in g]
+        _, mis = engine.forward(list(shots), obs, keep=True, want_rec=False)
+        ctx.engine = engine
         return torch.tensor(float(np.sum(mis)), dtype=torch.float64)
 
     @staticmethod
     def backward(ctx, gout):
-        gl, gm, gr = (gout * x for x in ctx.grads)
-        return gl, gm, gr, None, None, None
+        eng = ctx.engine
+        g = eng.backward(sum_shots=True)
+        gl, gm, gr = (gout * torch.from_numpy(_to_grid(x, eng.p)) for x in g)
+        return gl, gm, gr, None, None, None, None
 
 
-def misfit(lam, mu, rho, engine, shots, obs):
-    return FWIMisfit.apply(lam, mu, rho, engine, shots, obs)
+def misfit(lam, mu, rho, engine, shots, obs, mode="exact"):
+    return FWIMisfit.apply(lam, mu, rho, engine, shots, obs, mode)

@@ -1,7 +1,9 @@
 """Build ``libfwi_psv.so`` (the sm_103a engine + C ABI) in-tree with nvcc.
 
-Output: ``cuda_fwi_gb300/_lib/libfwi_psv.so`` and the INI-driven host program
-``cuda_fwi_gb300/_lib/fwi_run`` (app/, plain C++ against the C ABI).
+Output: ``cuda_fwi_gb300/_lib/libfwi_psv.so``, the INI-driven host program
+``cuda_fwi_gb300/_lib/fwi_run`` (app/, plain C++ against the C ABI) and
+``cuda_fwi_gb300/_lib/ref_driver``, a reference-style caller of the drop-in
+propagator symbols (app/ref_driver.cpp).
 Translation units are compiled in parallel and only when a source is newer
 than its object.
 """
@@ -28,6 +30,7 @@ UNITS = ["fwi_engine.cu", "fwi_host.cpp", "fwi_refshim.cpp", "fwi_noalloc.cu", "
 HEADERS = ["fwi_kernels.cuh", "fwi_exact.cuh", "fwi_tma.cuh", "fwi_multi.cuh", "fwi_host.h"]
 APP_DIR = PKG / "app"
 APP = OUT_DIR / "fwi_run"
+REF_DRIVER = OUT_DIR / "ref_driver"
 
 
 def nvcc() -> str:
@@ -68,6 +71,9 @@ def build(force: bool = False, verbose_ptxas: bool = False, defines=(), out: Pat
     app_deps = [APP_DIR / "fwi_main.cpp", APP_DIR / "ini.hpp", ROOT / "include" / "fwi_psv.h", LIB]
     if force or not APP.exists() or APP.stat().st_mtime < max(p.stat().st_mtime for p in app_deps):
         build_app()
+    drv_deps = [APP_DIR / "ref_driver.cpp", ROOT / "include" / "fwi_psv_ref.hpp", ROOT / "include" / "fwi_psv.h", LIB]
+    if force or not REF_DRIVER.exists() or REF_DRIVER.stat().st_mtime < max(p.stat().st_mtime for p in drv_deps):
+        build_ref_driver()
     if verbose_ptxas:
         print("\n".join(logs))
     return LIB
@@ -81,6 +87,17 @@ def build_app() -> Path:
           "-o", str(tmp), f"-L{OUT_DIR}", "-lfwi_psv", "-Wl,-rpath,$ORIGIN"])
     os.replace(tmp, APP)
     return APP
+
+
+def build_ref_driver() -> Path:
+    """A reference-style caller of the drop-in propagators (app/ref_driver.cpp):
+    host code compiled by nvcc (for the CUDA runtime it allocates with),
+    linked against libfwi_psv.so found next to it."""
+    tmp = REF_DRIVER.with_suffix(".tmp")
+    _run([nvcc(), "-O2", "-std=c++17", f"-I{ROOT / 'include'}", str(APP_DIR / "ref_driver.cpp"), "-o", str(tmp),
+          f"-L{OUT_DIR}", "-lfwi_psv", "-Xlinker", "-rpath,$ORIGIN"])
+    os.replace(tmp, REF_DRIVER)
+    return REF_DRIVER
 
 
 def _build_variant(defines, out: Path) -> Path:

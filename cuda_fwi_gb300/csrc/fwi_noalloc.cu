@@ -15,6 +15,12 @@
 // process exits.  All calls share it and it keeps the last call's contents, so
 // the flag is cleared at the start of every call, and calls that overlap on the
 // GPU (different streams or host threads at the same time) race on it.
+// Its device address is looked up once per device (with that device current)
+// and kept for the life of the process: a caller that destroys the device's
+// primary context between calls (cudaDeviceReset) invalidates it, so such a
+// caller must not use this entry point afterwards.  Every call ends with a
+// copy into host memory and a wait on its stream, so it cannot be made while
+// that stream is being captured into a CUDA graph.
 #include <cuda_runtime.h>
 
 #include <cstddef>
@@ -101,6 +107,12 @@ extern "C" int fwi_psv_misfit_noalloc(const float* d_syn, const float* d_obs, in
         return fwi::fail(FWI_ERR_INVALID, "fwi_psv_misfit_noalloc: " + std::to_string(nrows) +
                                               " traces exceed the fixed scratch of " +
                                               std::to_string(kMaxRows) + " (FWI_NOALLOC_MAX_ROWS)");
+    // an error left pending by earlier, unrelated work is reported as such
+    // (and left for its owner: peek, do not clear)
+    cudaError_t pending = cudaPeekAtLastError();
+    if (pending != cudaSuccess)
+        return fwi::fail(FWI_ERR_CUDA, std::string("fwi_psv_misfit_noalloc: a CUDA error was pending before the "
+                                                   "call: ") + cudaGetErrorString(pending));
     Scratch* s = nullptr;
     int st = scratch_for_current_device(&s);
     if (st != FWI_OK) return st;

@@ -8,26 +8,50 @@
 #include <cstdio>
 #include <vector>
 
+#include <string>
+
 #include "../../include/fwi_psv.h"
 #include "../../include/fwi_psv_ref.hpp"
+#include "fwi_host.h"
 
 namespace {
+
+// Status of the calling thread's last drop-in call (the reference signatures
+// return void; fwi_psv_ref_status() hands it to callers that want it).
+thread_local int g_ref_status = FWI_OK;
 
 double* flat(real_sim** p) { return p ? p[0] : nullptr; }
 double* flat3(real_sim*** p) { return (p && p[0]) ? p[0][0] : nullptr; }
 
 void report(int status, const char* where) {
+    g_ref_status = status;
     if (status != FWI_OK)
         std::fprintf(stderr, "fwi_psv: %s failed: %s (%s)\n", where, fwi_psv_strerror(status),
                      fwi_psv_last_error());
 }
 
-void to_device(double* dst, const double* src, size_t n) {
-    if (dst && src && n) cudaMemcpy(dst, src, n * sizeof(double), cudaMemcpyHostToDevice);
-}
-void from_device(double* dst, const double* src, size_t n) {
-    if (dst && src && n) cudaMemcpy(dst, src, n * sizeof(double), cudaMemcpyDeviceToHost);
-}
+// Copies between the caller's host arrays and its FP64 device buffers.  The
+// first failing copy is recorded (fwi_psv_last_error, fwi_psv_ref_status) and
+// every later copy of the same call is skipped.
+struct Copier {
+    const char* where;
+    int status = FWI_OK;
+    void run(double* dst, const double* src, size_t n, cudaMemcpyKind kind, const char* what) {
+        if (status != FWI_OK || !dst || !src || !n) return;
+        const cudaError_t e = cudaMemcpy(dst, src, n * sizeof(double), kind);
+        if (e != cudaSuccess) {
+            status = fwi::fail(FWI_ERR_CUDA, std::string(where) + ": copy of " + what + " " +
+                                                 (kind == cudaMemcpyHostToDevice ? "to" : "from") +
+                                                 " the device failed: " + cudaGetErrorString(e));
+        }
+    }
+    void to_device(double* dst, const double* src, size_t n, const char* what) {
+        run(dst, src, n, cudaMemcpyHostToDevice, what);
+    }
+    void from_device(double* dst, const double* src, size_t n, const char* what) {
+        run(dst, src, n, cudaMemcpyDeviceToHost, what);
+    }
+};
 
 struct Sizes {
     size_t cells, xs, zs, store;
@@ -95,27 +119,29 @@ void forward_kernel_PSV_GPU(int ishot, int nt, int nzt, int nxt, int fpad, int p
         st[3], st[4]);
     report(rc, "forward_kernel_PSV_GPU");
     if (rc != FWI_OK) return;
-    to_device(d_vx, flat(vx), S.cells);
-    to_device(d_vz, flat(vz), S.cells);
-    to_device(d_sxx, flat(sxx), S.cells);
-    to_device(d_szx, flat(szx), S.cells);
-    to_device(d_szz, flat(szz), S.cells);
-    to_device(d_We, we.data(), S.cells);
-    to_device(d_mem_vx_x, flat(mem_vx_x), S.xs);
-    to_device(d_mem_vz_x, flat(mem_vz_x), S.xs);
-    to_device(d_mem_sxx_x, flat(mem_sxx_x), S.xs);
-    to_device(d_mem_szx_x, flat(mem_szx_x), S.xs);
-    to_device(d_mem_vx_z, flat(mem_vx_z), S.zs);
-    to_device(d_mem_vz_z, flat(mem_vz_z), S.zs);
-    to_device(d_mem_szz_z, flat(mem_szz_z), S.zs);
-    to_device(d_mem_szx_z, flat(mem_szx_z), S.zs);
+    Copier c{"forward_kernel_PSV_GPU"};
+    c.to_device(d_vx, flat(vx), S.cells, "vx");
+    c.to_device(d_vz, flat(vz), S.cells, "vz");
+    c.to_device(d_sxx, flat(sxx), S.cells, "sxx");
+    c.to_device(d_szx, flat(szx), S.cells, "szx");
+    c.to_device(d_szz, flat(szz), S.cells, "szz");
+    c.to_device(d_We, we.data(), S.cells, "We");
+    c.to_device(d_mem_vx_x, flat(mem_vx_x), S.xs, "mem_vx_x");
+    c.to_device(d_mem_vz_x, flat(mem_vz_x), S.xs, "mem_vz_x");
+    c.to_device(d_mem_sxx_x, flat(mem_sxx_x), S.xs, "mem_sxx_x");
+    c.to_device(d_mem_szx_x, flat(mem_szx_x), S.xs, "mem_szx_x");
+    c.to_device(d_mem_vx_z, flat(mem_vx_z), S.zs, "mem_vx_z");
+    c.to_device(d_mem_vz_z, flat(mem_vz_z), S.zs, "mem_vz_z");
+    c.to_device(d_mem_szz_z, flat(mem_szz_z), S.zs, "mem_szz_z");
+    c.to_device(d_mem_szx_z, flat(mem_szx_z), S.zs, "mem_szx_z");
     if (fwinv) {
-        to_device(d_fwi_vx, st[0], S.store);
-        to_device(d_fwi_vz, st[1], S.store);
-        to_device(d_fwi_sxx, st[2], S.store);
-        to_device(d_fwi_szx, st[3], S.store);
-        to_device(d_fwi_szz, st[4], S.store);
+        c.to_device(d_fwi_vx, st[0], S.store, "fwi_vx");
+        c.to_device(d_fwi_vz, st[1], S.store, "fwi_vz");
+        c.to_device(d_fwi_sxx, st[2], S.store, "fwi_sxx");
+        c.to_device(d_fwi_szx, st[3], S.store, "fwi_szx");
+        c.to_device(d_fwi_szz, st[4], S.store, "fwi_szz");
     }
+    report(c.status, "forward_kernel_PSV_GPU");
 }
 
 void adjoint_kernel_PSV_GPU(int ishot, int nt, int nzt, int nxt, int fpad, int ppad, real_sim dt,
@@ -153,12 +179,18 @@ void adjoint_kernel_PSV_GPU(int ishot, int nt, int nzt, int nxt, int fpad, int p
     std::vector<double> tmp;
     double* st[5] = {flat3(fwi_vx), flat3(fwi_vz), flat3(fwi_sxx), flat3(fwi_szx), flat3(fwi_szz)};
     double* dst[5] = {d_fwi_vx, d_fwi_vz, d_fwi_sxx, d_fwi_szx, d_fwi_szz};
+    Copier in{"adjoint_kernel_PSV_GPU"};
     if (fwinv && dst[0] && dst[1] && dst[2] && dst[3] && dst[4]) {
         tmp.assign(5 * S.store, 0.0);
+        static const char* names[5] = {"d_fwi_vx", "d_fwi_vz", "d_fwi_sxx", "d_fwi_szx", "d_fwi_szz"};
         for (int q = 0; q < 5; q++) {
             st[q] = tmp.data() + q * S.store;
-            from_device(st[q], dst[q], S.store);
+            in.from_device(st[q], dst[q], S.store, names[q]);
         }
+    }
+    if (in.status != FWI_OK) {
+        report(in.status, "adjoint_kernel_PSV_GPU");
+        return;
     }
     std::vector<double> we(S.cells), gtmp;
     double* g[3] = {flat(grad_lam), flat(grad_mu), flat(grad_rho)};
@@ -177,21 +209,25 @@ void adjoint_kernel_PSV_GPU(int ishot, int nt, int nzt, int nxt, int fpad, int p
         g[1], g[2]);
     report(rc, "adjoint_kernel_PSV_GPU");
     if (rc != FWI_OK) return;
-    to_device(d_vx, flat(vx), S.cells);
-    to_device(d_vz, flat(vz), S.cells);
-    to_device(d_sxx, flat(sxx), S.cells);
-    to_device(d_szx, flat(szx), S.cells);
-    to_device(d_szz, flat(szz), S.cells);
-    to_device(d_We, we.data(), S.cells);
-    to_device(d_mem_vx_x, flat(mem_vx_x), S.xs);
-    to_device(d_mem_vz_x, flat(mem_vz_x), S.xs);
-    to_device(d_mem_sxx_x, flat(mem_sxx_x), S.xs);
-    to_device(d_mem_szx_x, flat(mem_szx_x), S.xs);
-    to_device(d_mem_vx_z, flat(mem_vx_z), S.zs);
-    to_device(d_mem_vz_z, flat(mem_vz_z), S.zs);
-    to_device(d_mem_szz_z, flat(mem_szz_z), S.zs);
-    to_device(d_mem_szx_z, flat(mem_szx_z), S.zs);
-    to_device(d_grad_lam, g[0], ng);
-    to_device(d_grad_mu, g[1], ng);
-    to_device(d_grad_rho, g[2], ng);
+    Copier c{"adjoint_kernel_PSV_GPU"};
+    c.to_device(d_vx, flat(vx), S.cells, "vx");
+    c.to_device(d_vz, flat(vz), S.cells, "vz");
+    c.to_device(d_sxx, flat(sxx), S.cells, "sxx");
+    c.to_device(d_szx, flat(szx), S.cells, "szx");
+    c.to_device(d_szz, flat(szz), S.cells, "szz");
+    c.to_device(d_We, we.data(), S.cells, "We");
+    c.to_device(d_mem_vx_x, flat(mem_vx_x), S.xs, "mem_vx_x");
+    c.to_device(d_mem_vz_x, flat(mem_vz_x), S.xs, "mem_vz_x");
+    c.to_device(d_mem_sxx_x, flat(mem_sxx_x), S.xs, "mem_sxx_x");
+    c.to_device(d_mem_szx_x, flat(mem_szx_x), S.xs, "mem_szx_x");
+    c.to_device(d_mem_vx_z, flat(mem_vx_z), S.zs, "mem_vx_z");
+    c.to_device(d_mem_vz_z, flat(mem_vz_z), S.zs, "mem_vz_z");
+    c.to_device(d_mem_szz_z, flat(mem_szz_z), S.zs, "mem_szz_z");
+    c.to_device(d_mem_szx_z, flat(mem_szx_z), S.zs, "mem_szx_z");
+    c.to_device(d_grad_lam, g[0], ng, "grad_lam");
+    c.to_device(d_grad_mu, g[1], ng, "grad_mu");
+    c.to_device(d_grad_rho, g[2], ng, "grad_rho");
+    report(c.status, "adjoint_kernel_PSV_GPU");
 }
+
+extern "C" int fwi_psv_ref_status(void) { return g_ref_status; }

@@ -24,6 +24,23 @@ import numpy as np
 
 from . import _capi
 
+# Setup helpers (padding, Holberg table, CPML profile, Ricker wavelet, staggered
+# averages).  The default is the engine library's host code; any object with the
+# same five functions (total_grid, holberg, cpml_profile, wavelet,
+# average_parameters) can stand in, e.g. to build a problem in a process that
+# must not load the engine library.
+_setup = None
+
+
+def use_setup_helpers(helpers) -> None:
+    """Route every later Problem setup through `helpers` (None: the engine library)."""
+    global _setup
+    _setup = helpers
+
+
+def _h():
+    return _setup if _setup is not None else _capi
+
 
 @dataclass
 class Problem:
@@ -76,11 +93,11 @@ class Problem:
     name: str = ""
 
     def finalize(self) -> "Problem":
-        self.fpad, self.ppad, self.nxt, self.nzt = _capi.total_grid(
+        self.fpad, self.ppad, self.nxt, self.nzt = _h().total_grid(
             self.nx, self.nz, self.fdorder, self.npml, self.fsurf)
-        self.hc = _capi.holberg(self.fdorder, self.max_rel_err)
+        self.hc = _h().holberg(self.fdorder, self.max_rel_err)
         if self.npml > 0:
-            self.cpml = _capi.cpml_profile(self.npml, self.dx, self.fpml, self.npower,
+            self.cpml = _h().cpml_profile(self.npml, self.dx, self.fpml, self.npower,
                                            self.k_max_pml, self.rcoef, self.damp_v_pml, self.dt)
         else:
             self.cpml = {k: np.zeros(2) for k in ("a", "b", "K", "a_half", "b_half", "K_half")}
@@ -115,7 +132,7 @@ class Problem:
 
     def averaged(self):
         """mu_zx, rho_zp, rho_xp (fd_medium.cu:128-159) of the current lam/mu/rho."""
-        return _capi.average_parameters(self.mu, self.rho)
+        return _h().average_parameters(self.mu, self.rho)
 
     def zoff(self) -> int:
         """z offset from the physical grid to the padded one (fd_seismogram.cu:157-160)."""
@@ -141,7 +158,7 @@ class Problem:
         self.src_comp = np.full(n, comp, np.int32)
         self.src_shot = np.asarray(shot, np.int32)
         f0 = np.broadcast_to(np.asarray(f0, np.float64), (n,))
-        self.src_signal = np.stack([_capi.wavelet(self.nt, self.dt, amp, float(f), ts, 1) for f in f0]) \
+        self.src_signal = np.stack([_h().wavelet(self.nt, self.dt, amp, float(f), ts, 1) for f in f0]) \
             if n else np.zeros((0, self.nt))
         self.src_signal = np.ascontiguousarray(self.src_signal)
         self.nshots = int(self.src_shot.max()) + 1 if n else 1

@@ -400,9 +400,12 @@ int fwi_psv_multi_get_stats(fwi_psv_multi* m, fwi_psv_stats* out);
  * scratch is a fixed device array of FWI_NOALLOC_MAX_ROWS traces that every GPU
  * loading the library holds until exit; more traces return FWI_ERR_INVALID.
  * The first call on a device looks up the array's address with that device
- * current; make that first call before any stream capture.  All calls share
- * the array: calls that overlap on the GPU race.  Returns FWI_ERR_DIVERGED when
- * |diff| > 1e10, as the engine does. */
+ * current and keeps it for the life of the process (do not call
+ * cudaDeviceReset between calls).  Every call copies the misfit to the host and
+ * waits for its stream, so it cannot be called while that stream is being
+ * captured.  An error already pending on entry is returned as FWI_ERR_CUDA and
+ * left pending.  All calls share the array: calls that overlap on the GPU race.
+ * Returns FWI_ERR_DIVERGED when |diff| > 1e10, as the engine does. */
 #define FWI_NOALLOC_MAX_ROWS 65536
 int fwi_psv_misfit_noalloc(const float* d_syn, const float* d_obs, int nrows, int nt, double dt,
                            float* d_resid, double* misfit, void* stream);

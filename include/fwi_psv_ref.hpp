@@ -10,8 +10,10 @@
 // rows of `ishot` and the host wavefield receive the results; the FP64 device
 // buffers passed as d_* receive the final wavefield, d_We, the CPML memory and
 // the FWI storage ([nft][nfz][nfx], velocities divided by dt), and the adjoint
-// also fills d_grad_* and the host gradients.  Errors are reported through
-// fwi_psv_last_error() and make the call return early (no exit()).
+// also fills d_grad_* and the host gradients.  Errors (a failed engine call or
+// a failed copy into or out of the caller's d_* buffers) are printed to stderr,
+// recorded for fwi_psv_last_error() and fwi_psv_ref_status(), and make the call
+// return early (no exit()).
 #pragma once
 
 #include <vector>
@@ -72,3 +74,10 @@ void adjoint_kernel_PSV_GPU(int ishot, int nt, int nzt, int nxt, int fpad, int p
                             real_sim* d_grad_lam, real_sim* d_grad_mu, real_sim* d_grad_rho,
                             real_sim* d_lam, real_sim* d_mu, real_sim* d_mu_zx,
                             real_sim* d_rho_zp, real_sim* d_rho_xp);
+
+// Status of the calling thread's last forward_kernel_PSV_GPU /
+// adjoint_kernel_PSV_GPU call: FWI_OK (0) or an FWI_ERR_* code.  No counterpart
+// in the reference (whose propagators exit() on a CUDA error,
+// forward_kernel_PSV_GPU.cu:19-27); a reference-style driver that wants to
+// react to errors calls it after each propagator call.
+extern "C" int fwi_psv_ref_status(void);

@@ -2,9 +2,10 @@
 
 * ``build_oracle()`` compiles the C restatement ``oracle/fwi_oracle.c`` into
   ``oracle/_lib/libfwi_oracle.so`` with gcc (``-ffp-contract=off`` so x86-64
-  and aarch64 round identically).
+  and aarch64 round identically; ``-fopenmp`` where the compiler has it).
 * ``build_ref()`` compiles the reference's own CPU path from its sources where
-  they lie (``$FWI_REFERENCE_DIR``, default ``/root/reference``) together with
+  they lie (``$FWI_REFERENCE_DIR``, default: a ``reference`` checkout beside
+  this repository) together with
   ``oracle/ref_harness.cpp`` into ``oracle/_ref/libfwi_ref.so``.  Nothing is
   copied out of the reference tree; every output goes to ``oracle/_ref/``.
   ``CUDA_week2/fd_medium.cu`` holds a Latin-1 byte in a string literal that
@@ -54,13 +55,22 @@ def build_oracle(force: bool = False) -> Path:
         LIB_DIR.mkdir(exist_ok=True)
         cc = os.environ.get("CC", "gcc")
         tmp = ORACLE_SO.with_suffix(".so.tmp")
-        _run([cc, *CFLAGS, "-shared", "-o", str(tmp), str(src), "-lm"])
+        try:  # OpenMP cell loops (results do not depend on the thread count)
+            _run([cc, *CFLAGS, "-fopenmp", "-shared", "-o", str(tmp), str(src), "-lm"])
+        except RuntimeError:
+            _run([cc, *CFLAGS, "-shared", "-o", str(tmp), str(src), "-lm"])
         os.replace(tmp, ORACLE_SO)
     return ORACLE_SO
 
 
+def reference_root() -> Path:
+    """The reference checkout: $FWI_REFERENCE_DIR, else ``../reference`` beside this repository."""
+    env = os.environ.get("FWI_REFERENCE_DIR")
+    return Path(env) if env else HERE.parent.parent / "reference"
+
+
 def reference_dir() -> Path:
-    return Path(os.environ.get("FWI_REFERENCE_DIR", "/root/reference")) / "CUDA_week2"
+    return reference_root() / "CUDA_week2"
 
 
 def build_ref(force: bool = False) -> Path | None:

@@ -21,6 +21,7 @@ import numpy as np
 def _one(args):
     p, shot = args
     from oracle import oracle as O
+    O.set_threads(1)  # one core per process: the processes fill the host
     obs = np.zeros((p.nrec, p.nt))
     t0 = time.perf_counter()
     O.gradient(p, obs, shot)

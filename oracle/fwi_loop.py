@@ -117,41 +117,54 @@ def misfits(p, obs, shots, lam, mu, rho):
     return [O.misfit(p, obs, s, lam, mu, rho) for s in shots]
 
 
-def fwi_loop(p, obs, shots, iters, step0=0.01, precondition=True, trial="sum"):
-    """Summed-gradient order.  Returns (lam, mu, rho, log) with log entries
-    dict(misfit, step_length, trials, status)."""
+def fwi_loop(p, obs, shots, iters, step0=0.01, precondition=True, trial="sum", order="summed"):
+    """The inversion loop.  order "summed": one update per iteration from the
+    shot-summed gradient; "per_shot": the reference's order
+    (fd_wave_model.cu:777-955), one gradient, step search and update per shot
+    inside each iteration.  trial "sum": the search compares misfits summed over
+    all shots (with per-shot order its step-0 value is the all-shot sum at the
+    current model too); "last": the reference's search, which keeps the last
+    shot's trial misfit (fwi_step_length_estimation.cu:136) against the
+    gradient's own misfit.  The material constants C (medium_average) are taken
+    once per iteration; the staggered averages that each gradient and trial
+    forward use come from the model it runs on.  A failed search (status 1)
+    stops the loop with the model unchanged.  Returns (lam, mu, rho, log) with
+    one entry dict(misfit, step_length, trials, status) per update."""
     lam, mu, rho = p.lam.copy(), p.mu.copy(), p.rho.copy()
     step = step0
     log = []
+    groups = [list(shots)] if order == "summed" else [[s] for s in shots]
     for _ in range(iters):
         c = [float(np.mean(x)) for x in (lam, mu, rho)]
-        g = [np.zeros((p.nfz, p.nfx)) for _ in range(3)]
-        L0 = 0.0
-        for s in shots:
-            J, gs, fw, ad = O.gradient(p, obs, s, lam, mu, rho)
-            L0 += J
-            if precondition:
-                gs = scale_gradients(p, list(gs), fw["We"], ad["We"], c)
-            for i in range(3):
-                g[i] += gs[i]
-        norms = [grad_norm(p, m, gi) for m, gi in zip((lam, mu, rho), g)]
+        for grp in groups:
+            g = [np.zeros((p.nfz, p.nfx)) for _ in range(3)]
+            L0 = 0.0
+            for s in grp:
+                J, gs, fw, ad = O.gradient(p, obs, s, lam, mu, rho)
+                L0 += J
+                if precondition:
+                    gs = scale_gradients(p, list(gs), fw["We"], ad["We"], c)
+                for i in range(3):
+                    g[i] += gs[i]
+            if order == "per_shot" and trial == "sum":
+                L0 = sum(misfits(p, obs, shots, lam, mu, rho))
+            norms = [grad_norm(p, m, gi) for m, gi in zip((lam, mu, rho), g)]
 
-        def model(est):
-            f = (est, est, 0.5 * est)
-            return [grad_update(p, m, gi, fi * ni, name)
-                    for m, gi, fi, ni, name in zip((lam, mu, rho), g, f, norms, ("lam", "mu", "rho"))]
+            def model(est, g=g, norms=norms, cur=(lam, mu, rho)):
+                f = (est, est, 0.5 * est)
+                return [grad_update(p, m, gi, fi * ni, name)
+                        for m, gi, fi, ni, name in zip(cur, g, f, norms, ("lam", "mu", "rho"))]
 
-        def trial_fn(est):
-            mis = misfits(p, obs, shots, *model(est))
-            return mis[-1] if trial == "last" else sum(mis)
+            def trial_fn(est, model=model):
+                mis = misfits(p, obs, shots, *model(est))
+                return mis[-1] if trial == "last" else sum(mis)
 
-        opt, calls, status, _ = step_search(step, L0, trial_fn)
-        entry = dict(misfit=L0, step_length=opt if status != 1 else 0.0, trials=calls, status=status)
-        log.append(entry)
-        if status == 1:
-            break
-        lam, mu, rho = model(opt)
-        step = opt
+            opt, calls, status, _ = step_search(step, L0, trial_fn)
+            log.append(dict(misfit=L0, step_length=opt if status != 1 else 0.0, trials=calls, status=status))
+            if status == 1:
+                return lam, mu, rho, log
+            lam, mu, rho = model(opt)
+            step = opt
     return lam, mu, rho, log
 
 

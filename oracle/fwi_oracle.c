@@ -12,8 +12,28 @@
 #include <stdlib.h>
 #include <stddef.h>
 #include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 
 #define IX2(p, iz, ix, pitch) (p)[(size_t)(iz) * (size_t)(pitch) + (size_t)(ix)]
+
+/* Grids below this many cells run their cell loops on one thread (a parallel
+ * region per pass costs more than it saves there). */
+#define ORC_PAR(g) ((size_t)(g)->nzt * (size_t)(g)->nxt >= 65536)
+
+/* Threads of the cell loops (OpenMP builds; every cell of a pass is computed
+ * by one thread from values no thread of that pass writes, so the results do
+ * not depend on the thread count).  n <= 0: the OpenMP default. */
+int orc_set_threads(int n) {
+#ifdef _OPENMP
+    if (n > 0) omp_set_num_threads(n);
+    return omp_get_max_threads();
+#else
+    (void)n;
+    return 1;
+#endif
+}
 
 int orc_nft(int nt, int fwi_dt) { return 1 + (nt - 1) / fwi_dt; }
 int orc_nfz(const orc_fwi* f) { return 1 + (f->z2 - f->z1) / f->fwi_dz; }
@@ -187,6 +207,7 @@ static void stress_pass(const orc_grid* g, const orc_medium* m, orc_wave* w) {
     double hx[7], hz[7];
     for (int k = 1; k <= fpad; k++) { hx[k] = dxi * g->hc[k]; hz[k] = dzi * g->hc[k]; }
     const int nz1 = fpad, nz2 = nzt - fpad, nx1 = fpad, nx2 = nxt - fpad;
+#pragma omp parallel for schedule(static) if (ORC_PAR(g))
     for (int iz = nz1; iz < nz2; iz++) {
         for (int ix = nx1; ix < nx2; ix++) {
             size_t c = (size_t)iz * nxt + ix;
@@ -246,6 +267,7 @@ static void stress_pass(const orc_grid* g, const orc_medium* m, orc_wave* w) {
         }
     }
     if (g->fsurf) {
+#pragma omp parallel for schedule(static) if (ORC_PAR(g))
         for (int ix = nx1; ix < nx2; ix++)
             for (int sz = 1; sz <= fpad; sz++) {
                 IX2(w->szx, fpad - sz, ix, nxt) = -IX2(w->szx, fpad + sz, ix, nxt);
@@ -263,6 +285,7 @@ static void velocity_pass(const orc_grid* g, const orc_medium* m, orc_wave* w) {
     double hx[7], hz[7];
     for (int k = 1; k <= fpad; k++) { hx[k] = dxi * g->hc[k]; hz[k] = dzi * g->hc[k]; }
     const int nz1 = fpad, nz2 = nzt - fpad, nx1 = fpad, nx2 = nxt - fpad;
+#pragma omp parallel for schedule(static) if (ORC_PAR(g))
     for (int iz = nz1; iz < nz2; iz++) {
         for (int ix = nx1; ix < nx2; ix++) {
             size_t c = (size_t)iz * nxt + ix;
@@ -388,13 +411,60 @@ int orc_forward(int ishot, const orc_grid* g, const orc_medium* m, orc_wave* w,
     return 0;
 }
 
+/* One reverse step of orc_adjoint at time step it (adjoint_kernel_PSV_GPU.cu:818-1087):
+ * ux/uz integration, the correlation gradient from the forward fields of frame
+ * `frame` of the storage arrays st[5] (vx/dt, vz/dt, sxx, szx, szz; each
+ * [frames][nfz][nfx]) when it is a sampled step, the stress and velocity passes
+ * and the injection of adj_signal.  Shared by the stored-wavefield and the
+ * checkpointed gradients, so both run the same statements. */
+static void ref_adjoint_step(int ishot, const orc_grid* g, const orc_medium* m, orc_wave* w, double* ux,
+                             double* uz, const orc_seis* adj, const double* adj_signal, const orc_fwi* f,
+                             const double* const st[5], int it, int frame, double* grad_lam, double* grad_mu,
+                             double* grad_rho) {
+    const int nxt = g->nxt, nzt = g->nzt, nt = g->nt, fpad = g->fpad;
+    const double dt = g->dt;
+    const int nfz = orc_nfz(f), nfx = orc_nfx(f);
+#pragma omp parallel for schedule(static) if (ORC_PAR(g))
+    for (int iz = fpad; iz < nzt - fpad; iz++)
+        for (int ix = fpad; ix < nxt - fpad; ix++) {
+            size_t c = (size_t)iz * nxt + ix;
+            uz[c] += dt * w->vz[c];
+            ux[c] += dt * w->vx[c];
+        }
+    if (f->fwinv && !(it % f->fwi_dt)) {
+        const double *fvx = st[0], *fvz = st[1], *fsxx = st[2], *fszx = st[3], *fszz = st[4];
+#pragma omp parallel for schedule(static) if (ORC_PAR(g))
+        for (int iz = f->z1; iz < f->z2; iz += f->fwi_dz) {
+            int zf = (iz - f->z1) / f->fwi_dz;
+            for (int ix = f->x1; ix < f->x2; ix += f->fwi_dx) {
+                int xf = (ix - f->x1) / f->fwi_dx;
+                size_t o = ((size_t)frame * nfz + zf) * nfx + xf, c = (size_t)iz * nxt + ix;
+                size_t gi = (size_t)zf * nfx + xf;
+                double lam = m->lam[c], mu = m->mu[c];
+                double s1 = (fsxx[o] + fszz[o]) * (w->sxx[c] + w->szz[c]) * 0.25 /
+                            ((lam + mu) * (lam + mu));
+                double s2 = (fsxx[o] - fszz[o]) * (w->sxx[c] - w->szz[c]) / (mu * mu);
+                double s3 = (fszx[o] * w->szx[c]) / (mu * mu);
+                double s4 = ux[c] * fvx[o] + uz[c] * fvz[o];
+                grad_lam[gi] += f->fwi_dt * dt * s1;
+                grad_mu[gi] += f->fwi_dt * dt * (s3 + s1 + s2);
+                grad_rho[gi] -= f->fwi_dt * dt * s4;
+            }
+        }
+    }
+    stress_pass(g, m, w);
+    velocity_pass(g, m, w);
+    for (int is = 0; adj && is < adj->n; is++)
+        if (adj->shot[is] == ishot && adj->comp[is] == 2)
+            IX2(w->vz, adj->z[is], adj->x[is], nxt) += adj_signal[(size_t)is * nt + it];
+}
+
 int orc_adjoint(int ishot, const orc_grid* g, const orc_medium* m, orc_wave* w,
                 const orc_seis* adj, const double* adj_signal, const orc_fwi* f,
                 double* grad_lam, double* grad_mu, double* grad_rho) {
     int rc = check_grid(g);
     if (rc) return rc;
-    const int nxt = g->nxt, nzt = g->nzt, nt = g->nt, fpad = g->fpad;
-    const double dt = g->dt;
+    const int nxt = g->nxt, nzt = g->nzt, nt = g->nt;
     reset_wave(g, w);
     size_t n = (size_t)nzt * nxt;
     double* ux = (double*)calloc(n, sizeof(double));
@@ -404,39 +474,10 @@ int orc_adjoint(int ishot, const orc_grid* g, const orc_medium* m, orc_wave* w,
     memset(grad_lam, 0, (size_t)nfz * nfx * sizeof(double));
     memset(grad_mu, 0, (size_t)nfz * nfx * sizeof(double));
     memset(grad_rho, 0, (size_t)nfz * nfx * sizeof(double));
-    for (int it = nt - 1; it >= 0; it--) {
-        for (int iz = fpad; iz < nzt - fpad; iz++)
-            for (int ix = fpad; ix < nxt - fpad; ix++) {
-                size_t c = (size_t)iz * nxt + ix;
-                uz[c] += dt * w->vz[c];
-                ux[c] += dt * w->vx[c];
-            }
-        if (f->fwinv && !(it % f->fwi_dt)) {
-            int tf = it / f->fwi_dt;
-            for (int iz = f->z1; iz < f->z2; iz += f->fwi_dz) {
-                int zf = (iz - f->z1) / f->fwi_dz;
-                for (int ix = f->x1; ix < f->x2; ix += f->fwi_dx) {
-                    int xf = (ix - f->x1) / f->fwi_dx;
-                    size_t o = ((size_t)tf * nfz + zf) * nfx + xf, c = (size_t)iz * nxt + ix;
-                    size_t gi = (size_t)zf * nfx + xf;
-                    double lam = m->lam[c], mu = m->mu[c];
-                    double s1 = (f->sxx[o] + f->szz[o]) * (w->sxx[c] + w->szz[c]) * 0.25 /
-                                ((lam + mu) * (lam + mu));
-                    double s2 = (f->sxx[o] - f->szz[o]) * (w->sxx[c] - w->szz[c]) / (mu * mu);
-                    double s3 = (f->szx[o] * w->szx[c]) / (mu * mu);
-                    double s4 = ux[c] * f->vx[o] + uz[c] * f->vz[o];
-                    grad_lam[gi] += f->fwi_dt * dt * s1;
-                    grad_mu[gi] += f->fwi_dt * dt * (s3 + s1 + s2);
-                    grad_rho[gi] -= f->fwi_dt * dt * s4;
-                }
-            }
-        }
-        stress_pass(g, m, w);
-        velocity_pass(g, m, w);
-        for (int is = 0; adj && is < adj->n; is++)
-            if (adj->shot[is] == ishot && adj->comp[is] == 2)
-                IX2(w->vz, adj->z[is], adj->x[is], nxt) += adj_signal[(size_t)is * nt + it];
-    }
+    const double* const st[5] = {f->vx, f->vz, f->sxx, f->szx, f->szz};
+    for (int it = nt - 1; it >= 0; it--)
+        ref_adjoint_step(ishot, g, m, w, ux, uz, adj, adj_signal, f, st, it, it / f->fwi_dt, grad_lam, grad_mu,
+                         grad_rho);
     free(ux);
     free(uz);
     return 0;
@@ -833,4 +874,108 @@ int orc_exact_gradient(int ishot, const orc_grid* g, const double* lam, const do
     if (misfit) *misfit = J;
     free(mzx); free(chk); free(seg); free(adj); free(we); free(gavg); free(recs);
     return 0;
+}
+
+/* ---------------------------------------------------------------------------
+ * The reference's gradient of one shot (orc_forward with storage, then
+ * orc_l2_adjoint_sources on the shot's receivers, then orc_adjoint) with the
+ * forward wavefield held as full states every `interval` steps instead of the
+ * whole storage: the backward restores the state at the start of each segment,
+ * re-runs the segment's forward steps keeping their sampled window fields, and
+ * runs the segment's adjoint steps from them.  The statements and their order
+ * are those of the stored sequence, so the results are bit-identical; memory is
+ * ceil(nt/interval) states plus interval frames of window samples (a config-3
+ * shot: ~2.5 GB instead of 73 GB).
+ * ------------------------------------------------------------------------- */
+int orc_gradient_ckpt(int ishot, const orc_grid* g, const orc_medium* m, const orc_seis* src,
+                      const double* src_signal, const orc_seis* rec, const double* obs, double* rec_signal,
+                      const orc_fwi* f, int interval, double* misfit, double* grad_lam, double* grad_mu,
+                      double* grad_rho, double* we_fwd, double* we_adj) {
+    int rc = check_grid(g);
+    if (rc) return rc;
+    if (!f || !f->fwinv || interval < 1) return -5;
+    const int nxt = g->nxt, nt = g->nt;
+    const st_sizes s = state_sizes(g);
+    const int nseg = (nt + interval - 1) / interval;
+    const int nfz = orc_nfz(f), nfx = orc_nfx(f);
+    const size_t nf = (size_t)nfz * nfx;
+    double* snaps = (double*)malloc((size_t)nseg * s.total * sizeof(double));
+    double* work = (double*)calloc(s.total, sizeof(double));
+    double* we = (double*)calloc(s.n, sizeof(double));
+    double* seg = (double*)malloc((size_t)interval * 5 * nf * sizeof(double));
+    double* ux = (double*)calloc(s.n, sizeof(double));
+    double* uz = (double*)calloc(s.n, sizeof(double));
+    double* adjst = (double*)calloc(s.total, sizeof(double));
+    double* adjwe = (double*)calloc(s.n, sizeof(double));
+    double* res = (double*)calloc((size_t)(rec ? rec->n : 0) * nt + 1, sizeof(double));
+    if (!snaps || !work || !we || !seg || !ux || !uz || !adjst || !adjwe || !res) {
+        free(snaps); free(work); free(we); free(seg); free(ux); free(uz); free(adjst); free(adjwe); free(res);
+        return -4;
+    }
+    orc_wave w;
+    wave_view(g, work, we, &w);
+    /* forward sweep from rest: a state every `interval` steps, seismograms */
+    for (int it = 0; it < nt; it++) {
+        if (it % interval == 0) memcpy(snaps + (size_t)(it / interval) * s.total, work, s.total * sizeof(double));
+        stress_pass(g, m, &w);
+        velocity_pass(g, m, &w);
+        for (int is = 0; src && is < src->n; is++)
+            if (src->shot[is] == ishot && src->comp[is] == 2)
+                IX2(w.vz, src->z[is], src->x[is], nxt) += src_signal[(size_t)is * nt + it];
+        for (int ir = 0; rec && ir < rec->n; ir++)
+            if (rec->shot[ir] == ishot && rec->comp[ir] == 2)
+                rec_signal[(size_t)ir * nt + it] = IX2(w.vz, rec->z[ir], rec->x[ir], nxt);
+    }
+    if (we_fwd) memcpy(we_fwd, we, s.n * sizeof(double));
+    /* residual and misfit of the shot's receivers (calculate_l2_adjoint_sources) */
+    double J = 0.0;
+    int blow = 0;
+    for (int ir = 0; rec && ir < rec->n; ir++) {
+        if (rec->shot[ir] != ishot || rec->comp[ir] != 2) continue;
+        for (int it = 0; it < nt; it++) {
+            size_t i = (size_t)ir * nt + it;
+            double diff = rec_signal[i] - obs[i];
+            J += 0.5 * g->dt * diff * diff;
+            res[i] = diff;
+            if (fabs(diff) > 1.0e+10) blow = 1;
+        }
+    }
+    *misfit = J;
+    /* backward: segments from the last one down, each recomputed from its state */
+    orc_wave wa, wf;
+    wave_view(g, adjst, adjwe, &wa);
+    memset(grad_lam, 0, nf * sizeof(double));
+    memset(grad_mu, 0, nf * sizeof(double));
+    memset(grad_rho, 0, nf * sizeof(double));
+    double* st[5];
+    for (int q = 0; q < 5; q++) st[q] = seg + (size_t)q * interval * nf;
+    for (int sgi = nseg - 1; sgi >= 0; sgi--) {
+        const int t0 = sgi * interval, t1 = (t0 + interval < nt) ? t0 + interval : nt;
+        memcpy(work, snaps + (size_t)sgi * s.total, s.total * sizeof(double));
+        wave_view(g, work, we, &wf);
+        for (int it = t0; it < t1; it++) {
+            if (!(it % f->fwi_dt)) {
+                const int fr = it - t0;
+                for (int iz = f->z1; iz < f->z2; iz += f->fwi_dz) {
+                    int zf = (iz - f->z1) / f->fwi_dz;
+                    for (int ix = f->x1; ix < f->x2; ix += f->fwi_dx) {
+                        int xf = (ix - f->x1) / f->fwi_dx;
+                        size_t o = ((size_t)fr * nfz + zf) * nfx + xf, c = (size_t)iz * nxt + ix;
+                        st[2][o] = wf.sxx[c];
+                        st[3][o] = wf.szx[c];
+                        st[4][o] = wf.szz[c];
+                        st[0][o] = wf.vx[c] / g->dt;
+                        st[1][o] = wf.vz[c] / g->dt;
+                    }
+                }
+            }
+            if (it + 1 < t1) fwd_step(g, m, &wf, it, ishot, src, src_signal);
+        }
+        const double* const cst[5] = {st[0], st[1], st[2], st[3], st[4]};
+        for (int it = t1 - 1; it >= t0; it--)
+            ref_adjoint_step(ishot, g, m, &wa, ux, uz, rec, res, f, cst, it, it - t0, grad_lam, grad_mu, grad_rho);
+    }
+    if (we_adj) memcpy(we_adj, adjwe, s.n * sizeof(double));
+    free(snaps); free(work); free(we); free(seg); free(ux); free(uz); free(adjst); free(adjwe); free(res);
+    return blow ? 1 : 0;
 }

@@ -78,6 +78,11 @@ def lib():
         L.orc_grad_update.restype = None
         L.orc_calc_opt_step.argtypes = [dp, dp]
         L.orc_calc_opt_step.restype = C.c_double
+        L.orc_set_threads.argtypes = [C.c_int]
+        L.orc_set_threads.restype = C.c_int
+        L.orc_gradient_ckpt.argtypes = [C.c_int, C.POINTER(Grid), C.POINTER(Medium), C.POINTER(Seis), dp,
+                                        C.POINTER(Seis), dp, dp, C.POINTER(Fwi), C.c_int, dp, dp, dp, dp,
+                                        dp, dp]
         L.orc_exact_gradient.argtypes = [C.c_int, C.POINTER(Grid), dp, dp, dp, C.POINTER(Seis), dp,
                                          C.POINTER(Seis), dp, dp, dp, dp, dp]
         _lib = L
@@ -124,6 +129,32 @@ def total_grid(nx, nz, fdorder, npml, fsurf):
     o = [C.c_int() for _ in range(4)]
     lib().orc_total_grid(nx, nz, fdorder, npml, int(fsurf), *[C.byref(v) for v in o])
     return tuple(v.value for v in o)
+
+
+class setup_helpers:
+    """The five problem-setup functions of the engine library's host code
+    (same names and signatures as ``cuda_fwi_gb300._capi``), computed by the
+    oracle instead: ``problem.use_setup_helpers(oracle.setup_helpers)`` builds
+    problems in a process that never loads the engine library (the bench's
+    reference arm).  Bit-identical results (tests/test_capi_host.py)."""
+
+    total_grid = staticmethod(total_grid)
+
+    @staticmethod
+    def holberg(fdorder, max_rel_err=1):
+        return holberg(fdorder, max_rel_err)
+
+    @staticmethod
+    def cpml_profile(npml, dh, fpml, npower, k_max_pml, rcoef, damp_v_pml, dt):
+        return cpml(npml, dh, fpml, npower, k_max_pml, rcoef, damp_v_pml, dt)
+
+    @staticmethod
+    def wavelet(nt, dt, amp, fc, ts=0.0, shape=1):
+        return wavelet(nt, dt, amp, fc, ts, shape)
+
+    @staticmethod
+    def average_parameters(mu, rho):
+        return average(mu, mu, rho)  # the averages do not read lam
 
 
 class _Ctx:
@@ -243,6 +274,44 @@ def gradient(p, obs, shot=0, lam=None, mu=None, rho=None):
     J, res, _ = residual(fw["rec"], obs, p.dt, rows)
     ad = adjoint(p, shot, res, fw["store"], lam, mu, rho)
     return J, (ad["grad_lam"], ad["grad_mu"], ad["grad_rho"]), fw, ad
+
+
+def set_threads(n):
+    """Threads of the oracle's cell loops (results do not depend on it)."""
+    return lib().orc_set_threads(int(n))
+
+
+def ckpt_interval(p):
+    """Steps between the stored states of gradient_ckpt: about sqrt(nt x state
+    / window frame), which balances the states against one segment's frames."""
+    state = 5 * p.nzt * p.nxt + 8 * p.nxt * (p.npml + 1)
+    frame = 5 * p.nfz * p.nfx
+    return max(1, min(p.nt, int(round(np.sqrt(p.nt * state / frame)))))
+
+
+def gradient_ckpt(p, obs, shot=0, interval=None, lam=None, mu=None, rho=None):
+    """The same result as gradient() bit for bit (forward, residual, adjoint of
+    one shot) with the forward wavefield recomputed from a state every
+    `interval` steps instead of stored: memory for a full-size shot.
+    Returns (J, (grad_lam, grad_mu, grad_rho), rec, We_fwd, We_adj)."""
+    ctx = _Ctx(p, lam, mu, rho)
+    src, keep1 = ctx.seis(p.src_x, p.src_z, p.src_comp, p.src_shot)
+    rec, keep2 = ctx.seis(p.rec_x, p.rec_z, p.rec_comp, p.rec_shot)
+    sig = np.ascontiguousarray(p.src_signal, np.float64) if p.nsrc else np.zeros((1, p.nt))
+    ob = np.ascontiguousarray(obs, np.float64) if p.nrec else np.zeros((1, p.nt))
+    recs = np.zeros((max(p.nrec, 1), p.nt))
+    f = Fwi()
+    f.fwinv, f.fwi_dt, f.fwi_dx, f.fwi_dz = 1, p.fwi_dt, p.fwi_dx, p.fwi_dz
+    f.x1, f.x2, f.z1, f.z2 = p.x1, p.x2, p.z1, p.z2
+    g = [np.zeros((p.nfz, p.nfx)) for _ in range(3)]
+    wf, wa = np.zeros((p.nzt, p.nxt)), np.zeros((p.nzt, p.nxt))
+    J = C.c_double()
+    k = int(interval) if interval else ckpt_interval(p)
+    rc = lib().orc_gradient_ckpt(shot, C.byref(ctx.g), C.byref(ctx.m), C.byref(src), _d(sig), C.byref(rec),
+                                 _d(ob), _d(recs), C.byref(f), k, C.byref(J), *[_d(x) for x in g], _d(wf), _d(wa))
+    if rc < 0:
+        raise ValueError(f"orc_gradient_ckpt failed ({rc})")
+    return J.value, tuple(g), recs[: p.nrec], wf, wa
 
 
 def misfit(p, obs, shot=0, lam=None, mu=None, rho=None):

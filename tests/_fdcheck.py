@@ -11,6 +11,7 @@ import numpy as np
 def _pair(args):
     p, obs, name, iz, ix, eps = args
     from oracle import oracle as O
+    O.set_threads(1)  # one core per worker process
     vals = []
     for s in (1.0, -1.0):
         m = {"lam": p.lam.copy(), "mu": p.mu.copy(), "rho": p.rho.copy()}

@@ -18,7 +18,6 @@ Usage: python tests/golden/make_golden.py   (needs the reference sources)
 """
 from __future__ import annotations
 
-import os
 import sys
 from pathlib import Path
 
@@ -72,8 +71,7 @@ def main():
     np.savez_compressed(HERE / "ref_o2_fsurf.npz", **pack(p, 0, 0.5))
     p = P.small(fdorder=2, nx=44, nz=30, nt=140, npml=6, nshots=3, nrec=4, perturb=0.03, fwi=(4, 2, 2))
     np.savez_compressed(HERE / "ref_o2_multi.npz", **pack(p, 1, 0.8))
-    csv = Path(os.environ.get("FWI_REFERENCE_DIR", "/root/reference")) / \
-        "CUDA_week2/io/receiver/src_signal_1_1.csv"
+    csv = B.reference_root() / "CUDA_week2/io/receiver/src_signal_1_1.csv"
     first = csv.read_text().splitlines()[0]
     vals = np.array([float(v) for v in first.split(",") if v.strip()])
     np.savez_compressed(HERE / "ricker_kat.npz", signal=vals, amp=1000.0, fc=15.0, dt=0.2e-3, ts=0.0)

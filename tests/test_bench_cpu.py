@@ -38,6 +38,10 @@ def test_reference_arm_prints_one_json_line():
     assert cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["value"] == d["value"]
     assert "4 of 3000 time steps" in cb["sample"]
     assert "1000x500" in d["config"]["workload"]
+    # the same workload description as the engine's arm
+    assert d["config"] == bench.bench_config(bench.parse_args([]), P.config3(False, nshots=64), 1)
+    # the arm's process never loaded the engine library (its problem set-up is the oracle's)
+    assert d["product_library_mapped"] is False
 
 
 def test_algorithmic_bytes_per_cell():

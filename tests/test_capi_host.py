@@ -35,6 +35,7 @@ def test_cpp_reference_shims_exported():
     out = subprocess.run(["nm", "-D", "-C", str(_capi.LIB_PATH)], capture_output=True, text=True).stdout
     assert "forward_kernel_PSV_GPU(int, int, int, int, int, int, double" in out
     assert "adjoint_kernel_PSV_GPU(int, int, int, int, int, int, double" in out
+    assert " T fwi_psv_ref_status" in out
 
 
 def test_abi_version_and_strerror():

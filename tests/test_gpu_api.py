@@ -46,22 +46,44 @@ def test_gradient_subbatches_match_oracle(batch, bx):
     assert np.array_equal(mis, mis2)
 
 
-def test_autograd_wrapper():
+@pytest.mark.parametrize("mode", ["exact", "reference"])
+def test_autograd_wrapper(mode):
+    """forward = fwi_psv_forward (misfit only), backward = fwi_psv_backward;
+    the gradient equals the engine's fused gradient call in the same mode."""
     from cuda_fwi_gb300.autograd import misfit
     p, obs = _case(nshots=2)
     lam = torch.tensor(p.lam, requires_grad=True)
     mu = torch.tensor(p.mu, requires_grad=True)
     rho = torch.tensor(p.rho, requires_grad=True)
     with Engine(p) as eng:
-        J = misfit(lam, mu, rho, eng, [0, 1], obs)
+        J = misfit(lam, mu, rho, eng, [0, 1], obs, mode)
+        assert eng.stats()["adjoint_steps"] == 0  # the forward alone runs no adjoint
         (2.0 * J).backward()
+        assert eng.stats()["adjoint_steps"] == p.nt
+        eng.set_gradient_mode(mode)
         g, mis = eng.gradient([0, 1], obs)
     assert float(J.detach()) == pytest.approx(float(np.sum(mis)), rel=1e-12)
     win = (slice(p.z1, p.z2, p.fwi_dz), slice(p.x1, p.x2, p.fwi_dx))
     for t, gi in zip((lam, mu, rho), g):
         gw = t.grad.numpy()[win]
         # the window loop fills nfz-1 x nfx-1 entries when the range divides evenly
-        np.testing.assert_allclose(gw, 2.0 * gi[: gw.shape[0], : gw.shape[1]], rtol=0)
+        np.testing.assert_allclose(gw, 2.0 * gi[: gw.shape[0], : gw.shape[1]], rtol=1e-6)
+
+
+def test_autograd_exact_mode_is_the_misfit_derivative():
+    """In exact mode the wrapper's gradient matches the FP64 oracle's discrete
+    adjoint of the same misfit (relative L2 <= 1e-4)."""
+    from cuda_fwi_gb300.autograd import misfit
+    p, obs = _case(nshots=1, order=4)
+    lam = torch.tensor(p.lam, requires_grad=True)
+    mu = torch.tensor(p.mu, requires_grad=True)
+    rho = torch.tensor(p.rho, requires_grad=True)
+    with Engine(p) as eng:
+        misfit(lam, mu, rho, eng, [0], obs).backward()
+    J, gl, gm, gr = O.exact_gradient(p, obs, 0)
+    win = (slice(p.z1, p.z2, p.fwi_dz), slice(p.x1, p.x2, p.fwi_dx))
+    for t, go in zip((lam, mu, rho), (gl, gm, gr)):
+        assert rel_l2(t.grad.numpy()[win], go[win]) <= 1e-4
 
 
 def test_engine_reuses_graphs_across_shot_ids():

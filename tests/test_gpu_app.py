@@ -4,7 +4,10 @@ Forward modelling of tests/golden/ini/forward_small.ini: io/receiver/
 rec_signal.csv and the last szz snapshot against the oracle run on the same
 set-up (homogeneous medium with the reference's stiffer circle; CSV values
 carry 6 significant digits).  Full waveform inversion from a CSV observed-data
-file: two iterations, models written per iteration, the misfit decreasing.
+file: two iterations, models written per iteration, the misfit decreasing; and
+one iteration in the program's default order (the reference's: a gradient,
+step search and update per shot, last-shot trial misfit) against
+oracle/fwi_loop.py.
 """
 import re
 import subprocess
@@ -17,6 +20,7 @@ import pytest
 from conftest import rel_l2
 from cuda_fwi_gb300 import build as B
 from cuda_fwi_gb300 import problem as P
+from oracle import fwi_loop as FL
 from oracle import oracle as O
 
 pytestmark = pytest.mark.gpu
@@ -88,3 +92,46 @@ def test_fwi_mode_two_iterations(tmp_path):
             assert m.shape == (p.nzt, p.nxt)
     lam2 = _csv(tmp_path / "io/density_snap/lam_snap2.csv")
     assert not np.allclose(lam2, lam2[0, 0])  # the homogeneous start was updated
+
+
+def test_fwi_mode_default_order_matches_restatement(tmp_path):
+    """No fwi_order / trial_misfit keys: fwi_run takes the reference's per-shot
+    order with the last shot's trial misfit (fd_wave_model.cu:777-955,
+    fwi_step_length_estimation.cu:136); one iteration over the two shots gives
+    the restatement's misfits and step lengths and its model."""
+    p = _problem(nt=160)
+    obs = np.zeros((p.nrec, p.nt))
+    for s in (0, 1):
+        rows = O.shot_rows(p, s)
+        obs[rows] = O.forward(p, s)["rec"][rows]
+    # a homogeneous starting model (no circle): the program inverts for it
+    mu = 1732.0 ** 2 * 2000.0
+    start = p.with_model(np.full((p.nzt, p.nxt), 3000.0 ** 2 * 2000.0 - 2.0 * mu), np.full((p.nzt, p.nxt), mu),
+                         np.full((p.nzt, p.nxt), 2000.0))
+    # the program's default window: [ppad, nxt) x [ppad, nzt) (INI defaults moved onto the padded grid)
+    start = replace(start, x1=start.ppad, z1=start.ppad)
+    rows = O.shot_rows(p, 1)  # the last shot's data halfway to the start's: the search accepts steps
+    obs[rows] = 0.5 * (obs[rows] + O.forward(start, 1)["rec"][rows])
+    obs_path = tmp_path / "obs.csv"
+    obs_path.write_text("".join("".join(f"{v:.17g}, " for v in row) + "\n" for row in obs))
+    ini = (INI / "forward_small.ini").read_text()
+    ini = ini.replace("time = 0.2;", "nt = 160;").replace(
+        "full_waveform_inversion = 0;", "full_waveform_inversion = 1;\nmax_iteration = 1;\nmax_error = 0.0;\n"
+        "checkpoints = 8;")
+    ini = ini.replace("[receiver]\n", f"[receiver]\nmeasurement_records = 1;\nsignal_file = {obs_path}\n")
+    cfg = tmp_path / "fwi.ini"
+    cfg.write_text(ini)
+    r = subprocess.run([str(B.APP), str(cfg), "--out", str(tmp_path)], capture_output=True, text=True,
+                       timeout=600)
+    assert r.returncode in (0, 1), r.stderr + r.stdout
+    got = [(float(a), float(b), int(c)) for a, b, c in
+           re.findall(r"iteration 1: L2 = ([0-9.eE+-]+), step length = ([0-9.eE+-]+), trials = (\d+)", r.stdout)]
+    lam_r, mu_r, rho_r, log_r = FL.fwi_loop(start, obs, [0, 1], iters=1, step0=0.01, order="per_shot",
+                                            trial="last")
+    assert len(got) == len(log_r) == 2, r.stdout
+    for (mis, step, trials), want in zip(got, log_r):
+        assert trials == want["trials"]
+        assert mis == pytest.approx(want["misfit"], rel=1e-4)
+        assert step == pytest.approx(want["step_length"], rel=1e-3)
+    lam1 = _csv(tmp_path / "io/density_snap/lam_snap1.csv")
+    assert rel_l2(lam1 - start.lam, lam_r - start.lam) <= 1e-3  # CSV values carry 6 significant digits

@@ -8,6 +8,9 @@
   batched trial forwards, bounded update) follow oracle/fwi_loop.py: same
   trials and statuses, misfits within 1e-4, step lengths within 1e-3, and the
   model change within 1e-3 (relative L2).
+* The reference's own order -- a gradient, step search and update per shot,
+  with the last shot's trial misfit (fwi_run's defaults) or the all-shot sum --
+  follows the same restatement to the same bounds.
 """
 import numpy as np
 import pytest
@@ -82,3 +85,28 @@ def test_fwi_loop_follows_restatement():
     for got, want, start in ((lam, lam_r, p.lam), (mu, mu_r, p.mu), (rho, rho_r, p.rho)):
         assert rel_l2(got - start, want - start) <= 1e-3
     assert log[-1]["misfit"] < log[0]["misfit"]
+
+
+@pytest.mark.parametrize("trial", ["last", "sum"])
+def test_fwi_loop_per_shot_order_follows_restatement(trial):
+    """FWI_ORDER_PER_SHOT (fd_wave_model.cu:777-955) with FWI_TRIAL_LAST_SHOT
+    (fwi_step_length_estimation.cu:136) -- the reference's loop and fwi_run's
+    default -- and with the summed trial misfit.  The last shot's observed data
+    lie halfway between the starting and the true model's, so the reference's
+    comparison (the first shot's misfit against the last shot's trial misfits)
+    accepts steps and the loop makes four updates."""
+    p, t, obs = _case()
+    rows = O.shot_rows(p, 1)
+    obs[rows] = 0.5 * (obs[rows] + O.forward(p, 1)["rec"][rows])
+    lam_r, mu_r, rho_r, log_r = FL.fwi_loop(p, obs, [0, 1], iters=2, step0=0.01, order="per_shot", trial=trial)
+    with Engine(p) as eng:
+        eng.set_strategy("binomial", snapshots=8)
+        (lam, mu, rho), log = eng.fwi_run([0, 1], obs, max_iter=2, step_length=0.01, order="per_shot",
+                                          trial=trial, true_model=(t.lam, t.mu, t.rho))
+    assert len(log) == len(log_r) == 4
+    for a, b in zip(log, log_r):
+        assert a["trials"] == b["trials"] and a["status"] == b["status"]
+        assert a["misfit"] == pytest.approx(b["misfit"], rel=1e-4)
+        assert a["step_length"] == pytest.approx(b["step_length"], rel=1e-3)
+    for got, want, start in ((lam, lam_r, p.lam), (mu, mu_r, p.mu), (rho, rho_r, p.rho)):
+        assert rel_l2(got - start, want - start) <= 1e-3

@@ -10,6 +10,7 @@ import numpy as np
 import pytest
 
 from _fixtures import load
+from cuda_fwi_gb300 import problem as P
 from conftest import rel_l2
 from oracle import oracle as O
 from oracle import reference as R
@@ -108,3 +109,41 @@ def test_restatement_orders_consistent():
         errs[order] = O.forward(p, 0)["rec"]
     assert np.all(np.isfinite(errs[2])) and np.all(np.isfinite(errs[8]))
     assert 0.0 < rel_l2(errs[8], errs[2]) < 1.0
+
+
+@pytest.mark.parametrize("order,fsurf,fwi,interval,shot,nshots", [
+    (2, 0, (1, 1, 1), 7, 0, 1), (4, 1, (2, 1, 1), 1, 0, 1), (8, 0, (3, 2, 2), 50, 1, 2),
+    (8, 1, (1, 1, 1), 13, 0, 1), (6, 0, (1, 2, 3), 120, 0, 1), (12, 0, (2, 1, 1), 9, 2, 3)])
+def test_checkpointed_gradient_is_bit_identical(order, fsurf, fwi, interval, shot, nshots):
+    """orc_gradient_ckpt (states every `interval` steps, segments recomputed)
+    gives the stored-wavefield sequence's seismograms, misfit, gradients and
+    energies bit for bit, whatever the interval."""
+    kw = dict(fdorder=order, nx=40, nz=30, nt=120, npml=6, fsurf=fsurf, nshots=nshots, nrec=5,
+              perturb=0.05, fwi=fwi)
+    p, t = P.small(seed=2, **kw), P.small(seed=12, **kw)
+    obs = O.forward(t, shot)["rec"]
+    J, g, fw, ad = O.gradient(p, obs, shot)
+    Jc, gc, rec, wf, wa = O.gradient_ckpt(p, obs, shot, interval=interval)
+    rows = O.shot_rows(p, shot)
+    assert Jc == J
+    assert np.array_equal(rec[rows], fw["rec"][rows])
+    for a, b in zip(gc, g):
+        assert np.array_equal(a, b)
+    assert np.array_equal(wf, fw["We"]) and np.array_equal(wa, ad["We"])
+
+
+def test_oracle_threads_do_not_change_results():
+    p = P.small(fdorder=8, nx=48, nz=36, nt=90, npml=6, fsurf=1, nrec=5, perturb=0.05, seed=5)
+    obs = O.forward(P.small(fdorder=8, nx=48, nz=36, nt=90, npml=6, fsurf=1, nrec=5, perturb=0.05,
+                            seed=6), 0)["rec"]
+    n0 = O.set_threads(0)
+    try:
+        O.set_threads(1)
+        J1, g1, _, _ = O.gradient(p, obs, 0)
+        O.set_threads(max(2, n0))
+        J2, g2, _, _ = O.gradient(p, obs, 0)
+    finally:
+        O.set_threads(n0)
+    assert J1 == J2
+    for a, b in zip(g1, g2):
+        assert np.array_equal(a, b)
