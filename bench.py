@@ -53,7 +53,7 @@ def parse_args(argv):
     ap.add_argument("--shots", type=int, default=64)
     ap.add_argument("--snapshots", type=int, default=32)
     ap.add_argument("--nt", type=int, default=0, help="override nt (testing only)")
-    ap.add_argument("--plain-shots", type=int, default=1)
+    ap.add_argument("--plain-shots", type=int, default=3)
     ap.add_argument("--batch", type=int, default=0, help="shots per launch (0 = engine default)")
     ap.add_argument("--cpu-nt-sample", type=int, default=200)
     ap.add_argument("--no-uneven", dest="uneven", action="store_false",
@@ -210,9 +210,21 @@ def run_reference(args, rank):
     print(json.dumps(out), flush=True)
 
 
+def fused_step(block_x, fp):
+    """Whether the forward sweeps run the fused one-launch step (block_x 512,
+    fdorder <= 8)."""
+    return block_x == 512 and fp <= 4
+
+
 def kernel_names(block_x, fp):
-    """The four timed kernels of the thread mapping set_exec(block_x) selects."""
-    if block_x in (0, 256):  # TMA-staged tiles (the engine default)
+    """The four timed kernels of the thread mapping set_exec(block_x) selects
+    (entry 1 is None when the forward step is one fused launch)."""
+    if fused_step(block_x, fp):
+        return [f"step_fused_kernel<{fp}> (forward/recompute step: stress+velocity+CPML fused, TMA-staged "
+                f"120-column strips marched in 16-row chunks)", None,
+                f"adjoint_tma_kernel<{fp}> (adjoint stress+CPML+ux/uz+gradient, TMA-staged 128x8 tiles)",
+                f"velocity_tma_kernel<{fp}> (adjoint velocity+CPML+energy, TMA-staged 128x16 tiles)"]
+    if block_x in (0, 256, 512):  # TMA-staged tiles, two passes per forward step
         return [f"stress_tma_kernel<{fp}> (forward/recompute stress+CPML, TMA-staged 128x16 tiles)",
                 f"velocity_tma_kernel<{fp}> (forward/recompute velocity+CPML, TMA-staged 128x16 tiles)",
                 f"adjoint_tma_kernel<{fp}> (adjoint stress+CPML+ux/uz+gradient, TMA-staged 128x8 tiles)",
@@ -225,15 +237,20 @@ def kernel_names(block_x, fp):
             f"velocity_kernel<{fp},{vmap}> (adjoint velocity+CPML+energy)"]
 
 
-def algorithmic_bytes(p, B):
+def algorithmic_bytes(p, B, fused=False):
     """Minimal DRAM bytes of one launch over B shots (FP32): per-shot fields
-    once, shared materials once per launch, CPML memory of strip cells."""
+    once, shared materials once per launch, CPML memory of strip cells.  With
+    the fused step, entry 0 is the whole forward step (read and write the five
+    fields once, 40 B, the four CPML memories of a strip cell, 32 B, and all
+    five materials, 20 B) and entry 1 is 0."""
     fp = p.fpad
     nxi, nzi = p.nxt - 2 * fp, p.nzt - 2 * fp
     cells = nxi * nzi
     cpml_cells = 2 * p.npml * nzi + 2 * p.npml * nxi
     stress_fwd = B * (cells * (8 + 24) + cpml_cells * 16) + cells * 12
     vel_fwd = B * (cells * (12 + 16) + cpml_cells * 16) + cells * 8  # recompute sweeps: no energy
+    if fused:
+        stress_fwd, vel_fwd = B * (cells * 40 + cpml_cells * 32) + cells * 20, 0
     # adjoint: + ux,uz r/w (16) + 5 forward fields (20) + 3 gradients r/w (24) at a sampled step
     stress_adj = B * (cells * (8 + 24 + 16 + 20 + 24) + cpml_cells * 16) + cells * 12
     vel_adj = B * (cells * (12 + 16 + 8) + cpml_cells * 16) + cells * 8
@@ -350,13 +367,14 @@ def main():
     # ---- roofline: live per-kernel timing on one full sub-batch ----
     eng.forward(shots[:sub], obs, keep=True, want_rec=False)  # lays out a batch of `sub` shots
     ms = eng.time_kernels(reps=20)
-    b_sf, b_vf, b_sa, b_va = algorithmic_bytes(syn, sub)
-    counts = [syn.nt + recompute, syn.nt + recompute, syn.nt, syn.nt]
+    fused = fused_step(args.block_x, syn.fpad)
+    b_sf, b_vf, b_sa, b_va = algorithmic_bytes(syn, sub, fused)
+    counts = [syn.nt + recompute, 0 if fused else syn.nt + recompute, syn.nt, syn.nt]
     shares = [c * t for c, t in zip(counts, ms)]
     names = kernel_names(args.block_x, syn.fpad)
     dom = max(range(4), key=lambda i: shares[i])
     peak, peak_kind = peaks()
-    achieved = [b / (t / 1e3) / 1e9 for b, t in zip((b_sf, b_vf, b_sa, b_va), ms)]
+    achieved = [b / (t / 1e3) / 1e9 if t > 0 else 0.0 for b, t in zip((b_sf, b_vf, b_sa, b_va), ms)]
     traffic = None
     tfile = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tfile):
@@ -395,7 +413,7 @@ def main():
         torch.cuda.synchronize()
         pcs = time.perf_counter() - t0
         pc.close()
-        fb = [x / sub for x in algorithmic_bytes(syn, sub)]  # per shot, materials shared by a launch
+        fb = [x / sub for x in algorithmic_bytes(syn, sub, fused)]  # per shot, materials shared by a launch
         per_grad = (syn.nt + recompute) * (fb[0] + fb[1]) + syn.nt * (fb[2] + fb[3]) + \
             syn.nt * (syn.nxt - 2 * syn.fpad) * (syn.nzt - 2 * syn.fpad) * 8  # + energy of the recording sweep
         bound = peak * 1e9 / per_grad
@@ -501,7 +519,7 @@ def main():
                          "launch_ms": ms[dom], "algorithmic_bytes_per_launch": [b_sf, b_vf, b_sa, b_va][dom],
                          "all_kernels": {n.split(" ")[0] + ("_adj" if i >= 2 else "_fwd"):
                                          {"ms": ms[i], "GBps": achieved[i], "count_per_step": counts[i]}
-                                         for i, n in enumerate(names)}},
+                                         for i, n in enumerate(names) if n}},
             "plain": plain,
             "random_boundary": rbinfo,
             "uneven_batch": unev,

@@ -109,6 +109,8 @@ _SIGS = {
     "fwi_psv_wavefield": (C.c_int, [C.c_void_p, C.c_int, C.c_int, dp, dp, dp, dp, dp]),
     "fwi_psv_get_stats": (C.c_int, [C.c_void_p, C.POINTER(Stats)]),
     "fwi_psv_time_kernels": (C.c_int, [C.c_void_p, C.c_int, dp]),
+    "fwi_psv_set_wait_limit": (C.c_int, [C.c_void_p, C.c_double]),
+    "fwi_psv_debug_stall_next": (C.c_int, [C.c_void_p]),
     "fwi_psv_misfit_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_double,
                                          C.c_void_p, dp, C.c_void_p]),
     "fwi_psv_set_snapshots": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),

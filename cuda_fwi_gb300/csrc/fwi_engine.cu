@@ -28,6 +28,7 @@
 #include "fwi_exact.cuh"
 #include "fwi_kernels.cuh"
 #include "fwi_tma.cuh"
+#include "fwi_fused.cuh"
 
 namespace fwi {
 
@@ -63,7 +64,7 @@ __global__ void residual_kernel(const float* __restrict__ syn, const float* __re
         const double diff = (double)syn[o + t] - (double)ob[t];
         acc += half_dt * diff * diff;
         resid[o + t] = (float)diff;
-        big |= fabs(diff) > 1.0e10;
+        big |= !(fabs(diff) <= 1.0e10);  // also NaN / Inf
     }
     __shared__ double sh[256];
     __shared__ int sb;
@@ -80,6 +81,31 @@ __global__ void residual_kernel(const float* __restrict__ syn, const float* __re
         if (sb) atomicOr(blowup, 1);
     }
 }
+
+// Device watchdog: a non-finite value among samples [t0, t1) of the recorded
+// traces ([nrows][nt]) sets bit 16 of the error word (the host reports
+// FWI_ERR_DIVERGED; the TMA kernels of later steps return at once).
+__global__ void watch_traces_kernel(const float* __restrict__ rec, int nrows, int nt, int t0, int t1,
+                                    int* __restrict__ err) {
+    const int n = t1 - t0;
+    const size_t total = (size_t)nrows * n;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+        if (!isfinite(rec[(i / n) * nt + t0 + i % n])) {
+            atomicOr(err, 16);
+            return;
+        }
+    }
+}
+// the same over a flat array (the gradients)
+__global__ void watch_array_kernel(const float* __restrict__ a, size_t n, int* __restrict__ err) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        if (!isfinite(a[i])) {
+            atomicOr(err, 16);
+            return;
+        }
+    }
+}
+constexpr int kWatchSteps = 64;  // recorded steps between two watchdog checks
 
 // Source injection and receiver recording of one batch slot per block, after
 // a velocity pass that did neither (the TMA mapping): the injections of a
@@ -390,6 +416,32 @@ static TmaSet tma_for(int fp) {
     }
 }
 
+// Fused forward step (fwi_fused.cuh), fdorder 2..8.
+using FusedFn = void (*)(dim3, cudaStream_t, const FusedMaps&, const ItemDesc*, FusedGrid, int, unsigned, int*);
+template <int FP>
+static void t_fused(dim3 g, cudaStream_t s, const FusedMaps& m, const ItemDesc* it, FusedGrid fg, int step,
+                    unsigned flags, int* err) {
+    step_fused_kernel<FP><<<g, kFusedThreads, fused_smem<FP>(), s>>>(m, it, fg, step, flags, err);
+}
+template <int FP>
+static cudaError_t f_prepare() {
+    return cudaFuncSetAttribute(step_fused_kernel<FP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)fused_smem<FP>());
+}
+struct FusedSet {
+    FusedFn step = nullptr;
+    cudaError_t (*prepare)() = nullptr;
+};
+static FusedSet fused_for(int fp) {
+    switch (fp) {
+        case 1: return {t_fused<1>, f_prepare<1>};
+        case 2: return {t_fused<2>, f_prepare<2>};
+        case 3: return {t_fused<3>, f_prepare<3>};
+        case 4: return {t_fused<4>, f_prepare<4>};
+        default: return {};
+    }
+}
+
 // Forward steps a backward runs for a binomial plan over n units: from the
 // last checkpoint of the first sweep (placed while the forward records) to
 // the last unit, then every ADVANCE after that prefix, plus state n+1 of each
@@ -664,6 +716,17 @@ struct Engine {
     const AdjMaps* amap_cur = nullptr;  // forward fields of the adjoint pass (null: amap)
     TmaGrid tgrid{}, tgrid_a{};
     int grid_tma = 1, grid_tma_a = 1;
+    // Fused forward step (one launch per step, state double-buffered): the
+    // working state alternates between d_fwd and d_fwd2; per buffer k (the
+    // buffers of buf()) the maps the step reads from it.
+    bool fuse = false;  // set_exec: 512 the fused step, 0/256 the two TMA passes
+    FusedSet fset{};
+    DBuf d_fwd2;
+    std::vector<FusedMaps> fmaps_b;
+    FusedGrid fgrid{};
+    int grid_fused = 1;
+    unsigned long long wait_ns = kWaitNs;  // limit of the kernels' bounded waits
+    bool stall_next = false, stall_pending = false;  // test hook: one fused step whose wait runs out
     bool zero_mu = false;  // some interior cell has mu == 0 (exact mode unsupported)
     // energy-weight preconditioning of each shot's gradient (fd_wave_model.cu:1004-1052)
     bool pre_on = false;
@@ -759,7 +822,9 @@ struct Engine {
         ks = kernels_for(fpad, kmap);
         xs = exact_for(fpad);
         tset = tma_for(fpad);
+        fset = fused_for(fpad);
         if (kmap == 3) CUDA_TRY(tset.prepare());
+        if (kmap == 3 && fset.prepare) CUDA_TRY(fset.prepare());
         CUDA_TRY(cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, device));
         FWI_TRY(d_err.ensure(16));
         CUDA_TRY(cudaMemset(d_err.p, 0, 16));
@@ -782,6 +847,9 @@ struct Engine {
     bool store_mode() const { return strategy == FWI_STORE_FULL && !exact(); }
     bool random_mode() const { return strategy == FWI_STORE_RANDOM && !exact(); }
     bool state_source() const { return ckpt_mode() || random_mode(); }  // gradient reads the forward state
+    // The forward sweeps run the fused step (TMA mapping, fdorder <= 8; the
+    // exact adjoint keeps its in-place two-pass steps).
+    bool fused() const { return kmap == 3 && fuse && fset.step != nullptr && !exact(); }
     int unit() const { return exact() ? 1 : fwi_dt; }
     int nunits() const { return exact() ? nt : nft; }
 
@@ -924,7 +992,7 @@ struct Engine {
     size_t batch_bytes(int nb, int nslots, int strat) const {
         size_t f = 4;
         size_t b = 0;
-        b += 2 * (size_t)nb * state * f;        // fwd + adj state
+        b += (fused() ? 3 : 2) * (size_t)nb * state * f;  // fwd (+ second working buffer) + adj state
         b += 4 * (size_t)nb * field * f;        // ws, wr, ux, uz
         b += 3 * (size_t)nb * nf * f + 6 * nf * f;  // grads, sum, accumulator
         const bool ck = strat == FWI_STORE_BINOMIAL || (strat >= 0 && exact());
@@ -1024,6 +1092,13 @@ struct Engine {
         // buffers (capacity; addresses captured in graphs)
         FWI_TRY(grow(d_fwd, (size_t)cap * state * 4));
         FWI_TRY(grow(d_adj, (size_t)cap * state * 4));
+        if (fused()) {
+            // the second working buffer: cells no step writes (grid borders) must
+            // read as zero, so fresh memory is zeroed once
+            const size_t before = d_fwd2.bytes;
+            FWI_TRY(grow(d_fwd2, (size_t)cap * state * 4));
+            if (d_fwd2.bytes != before) CUDA_TRY(cudaMemsetAsync(d_fwd2.p, 0, d_fwd2.bytes, stream));
+        }
         FWI_TRY(grow(d_ws, (size_t)cap * field * 4));
         FWI_TRY(grow(d_wr, (size_t)cap * field * 4));
         FWI_TRY(grow(d_ux, (size_t)cap * field * 4));
@@ -1157,8 +1232,8 @@ struct Engine {
                 x.field = (long long)field;
             }
         }
-        if (copy_free()) {
-            const int nbuf = slots + 1;
+        if (copy_free() || fused()) {
+            const int nbuf = nbufs();
             std::vector<ItemDesc> itb((size_t)nbuf * B);
             for (int k = 0; k < nbuf; k++)
                 for (int b = 0; b < B; b++) fill_item(itb[(size_t)k * B + b], b, false, buf(k));
@@ -1180,6 +1255,68 @@ struct Engine {
         if (keep && ckpt_mode()) plan = plan_binomial(nunits(), slots, &plan_cost);
         return FWI_OK;
     }
+    // Maps of the fused step, per buffer it can read from.
+    int build_fused_maps() {
+        using G = FusedGeom<1>;  // box widths do not depend on the order; the heights do
+        const int vz_rows = kFusedTZ + 2 * fpad;
+        const size_t rb = (size_t)pitch * 4, sb = state * 4;
+        const float* mat = d_mat.as<float>();
+        const int nbuf = nbufs();
+        fmaps_b.assign(nbuf, FusedMaps{});
+        for (int k = 0; k < nbuf; k++) {
+            float* st = buf(k);
+            const int nb = k < slots ? B : Bcap;  // a checkpoint buffer holds B states
+            FusedMaps& F = fmaps_b[k];
+            FWI_TRY(make_map(&F.vx, st + F_VX * field, nxt, nzt, nb, rb, sb, G::VX, vz_rows));
+            FWI_TRY(make_map(&F.vz, st + F_VZ * field, nxt, nzt, nb, rb, sb, G::VX, vz_rows));
+            FWI_TRY(make_map(&F.sxx, st + F_SXX * field, nxt, nzt, nb, rb, sb, G::SX, kFusedTZ));
+            FWI_TRY(make_map(&F.szx, st + F_SZX * field, nxt, nzt, nb, rb, sb, G::SX, kFusedTZ));
+            FWI_TRY(make_map(&F.szz, st + F_SZZ * field, nxt, nzt, nb, rb, sb, G::SX, kFusedTZ));
+            FWI_TRY(make_map(&F.L, mat, nxt, nzt, 0, rb, 0, G::SX, kFusedTZ));
+            FWI_TRY(make_map(&F.M2, mat + field, nxt, nzt, 0, rb, 0, G::SX, kFusedTZ));
+            FWI_TRY(make_map(&F.MZ, mat + 2 * field, nxt, nzt, 0, rb, 0, G::SX, kFusedTZ));
+            FWI_TRY(make_map(&F.BX, mat + 3 * field, nxt, nzt, 0, rb, 0, G::W, kFusedTZ));
+            FWI_TRY(make_map(&F.BZ, mat + 4 * field, nxt, nzt, 0, rb, 0, G::W, kFusedTZ));
+        }
+        return FWI_OK;
+    }
+
+    // One fused forward step of the batch from the state of step `it` in buffer
+    // x to the state of step it+1 in buffer y (x != y), then the source/receiver
+    // events on y.
+    void fused_step(int x, int y, int it, unsigned flags, unsigned ev) {
+        FusedGrid fg = fgrid;
+        fg.msrc = (long long)(buf(x) - buf(y));
+        fg.stall = stall_pending ? 1 : 0;
+        stall_pending = false;
+        const ItemDesc* items = d_items_b.as<ItemDesc>() + (size_t)y * B;
+        fset.step(dim3(grid_fused), stream, fmaps_b[x], items, fg, it, flags, d_err.as<int>());
+        launches_now++;
+        if (ev) {
+            events_kernel<<<B, 256, 0, stream>>>(items, it, ev);
+            launches_now++;
+        }
+    }
+    // Recording forward steps [t0, t1) with the fused step, the state moving
+    // between the two working buffers (*cur: the one holding it); snapshots as
+    // forward_steps takes them.
+    void fused_steps(int t0, int t1, int* cur, bool record, bool store) {
+        for (int it = t0; it < t1; it++) {
+            const int other = *cur == slots ? slots + 1 : slots;
+            const unsigned f = ((store && it % fwi_dt == 0) ? FL_STORE : 0u) | (record ? FL_WE : 0u);
+            fused_step(*cur, other, it, f, FL_INJECT | (record ? FL_RECORD : 0u));
+            *cur = other;
+            if (record) watch(t0, it);
+            if (record && snap_interval > 0 && it % snap_interval == 0) {
+                const int k = it / snap_interval;
+                for (int b = 0; b < B; b++)
+                    cudaMemcpyAsync(d_snapshots.as<float>() + ((size_t)b * nsnap + k) * field,
+                                    buf(*cur) + (size_t)b * state + (size_t)snap_field * field, field * 4,
+                                    cudaMemcpyDeviceToDevice, stream);
+            }
+        }
+    }
+
     // Tensor maps of the TMA passes for the current buffers (addresses are
     // captured by value in the launches; buffers only grow, and a regrowth
     // drops every graph, so maps are rebuilt here with each batch layout).
@@ -1238,8 +1375,8 @@ struct Engine {
             FWI_TRY(make_map(&A.fszx, f + F_SZX * field, nxt, nzt, Bcap, rb, sb, kTmaTX, kAdjTZ));
             FWI_TRY(make_map(&A.fszz, f + F_SZZ * field, nxt, nzt, Bcap, rb, sb, kTmaTX, kAdjTZ));
         }
-        if (copy_free()) {
-            const int nbuf = slots + 1;
+        if (copy_free() || fused()) {
+            const int nbuf = nbufs();
             smaps_b.assign(nbuf, smaps[0]);
             vmaps_b.assign(nbuf, vmaps[0]);
             amaps_b.assign(nbuf, amap);
@@ -1268,6 +1405,7 @@ struct Engine {
                 (void)wza;
             }
         }
+        if (fused()) FWI_TRY(build_fused_maps());
         const int ntx = (nxt + kTmaTX - 1) / kTmaTX;
         const int ntz = (nzt - 2 * fpad + kTmaTZ - 1) / kTmaTZ;
         tgrid.nb = B;
@@ -1294,7 +1432,21 @@ struct Engine {
             tgrid.gzl = wz1;
             tgrid.gzh = wz2 - 1;
         }
+        tgrid.wait_ns = wait_ns;
         grid_tma = std::max(1, std::min(tgrid.ntiles, num_sms));
+        if (fused()) {
+            constexpr int Wf = FusedGeom<1>::W;  // owned columns per strip (the same for fdorder 2..8)
+            fgrid.nb = B;
+            fgrid.nunits = B * ((nxt + Wf - 1) / Wf);
+            fgrid.nch = (nzt - fpad + kFusedTZ - 1) / kFusedTZ;
+            fgrid.cxl = tgrid.cxl;
+            fgrid.cxh = tgrid.cxh;
+            fgrid.czl = tgrid.czl;
+            fgrid.czh = tgrid.czh;
+            fgrid.msrc = 0;
+            fgrid.wait_ns = wait_ns;
+            grid_fused = std::max(1, std::min(fgrid.nunits, num_sms));
+        }
         const int ntz_a = (nzt - 2 * fpad + kAdjTZ - 1) / kAdjTZ;
         tgrid_a = tgrid;
         tgrid_a.ntz = ntz_a;
@@ -1325,7 +1477,7 @@ struct Engine {
         return "|B" + std::to_string(B) + "|r" + std::to_string(rows.size()) + "|s" +
                std::to_string(slots) + "|st" + std::to_string(strategy) + "|t" + std::to_string(ntiles) +
                "|g" + std::to_string(grad_on ? 1 : 0) + "|m" + std::to_string(grad_mode) + "|rb" +
-               std::to_string(rb_active ? 1 : 0) + "|sn" +
+               std::to_string(rb_active ? 1 : 0) + "|fu" + std::to_string(fused() ? 1 : 0) + "|sn" +
                std::to_string(snap_interval) + "." + std::to_string(snap_field);
     }
 
@@ -1355,7 +1507,7 @@ struct Engine {
 
     size_t fixed_bytes() const { return d_mat.bytes + d_cpml.bytes + d_srcsig.bytes; }
     size_t allocated_bytes() const {
-        size_t t = d_fwd.bytes + d_adj.bytes + d_ws.bytes + d_wr.bytes + d_ux.bytes + d_uz.bytes +
+        size_t t = d_fwd.bytes + d_fwd2.bytes + d_adj.bytes + d_ws.bytes + d_wr.bytes + d_ux.bytes + d_uz.bytes +
                    d_grad.bytes + d_gsum.bytes + d_gacc.bytes + d_store.bytes + d_snap.bytes +
                    d_rec.bytes + d_obsf.bytes + d_resid.bytes + d_nxt.bytes + d_exact.bytes;
         return t;
@@ -1429,12 +1581,31 @@ struct Engine {
         launches_now += 2;
     }
 
-    // Error flags raised by the kernels (a bounded wait that timed out).
+    // Watchdog after recording step `it` (the recording sweep runs steps 0 ..
+    // nt-1 in order): every kWatchSteps steps and at the last step, the traces
+    // recorded since the previous check are scanned for NaN / Inf.
+    void watch(int t0, int it) {
+        (void)t0;
+        const int done = it + 1;
+        if (rows.empty() || (done % kWatchSteps != 0 && done != nt)) return;
+        const int a = done - (done % kWatchSteps ? done % kWatchSteps : kWatchSteps);
+        const size_t n = rows.size() * (size_t)(it + 1 - a);
+        const int blocks = (int)std::min<size_t>((n + 255) / 256, (size_t)num_sms * 4);
+        watch_traces_kernel<<<std::max(blocks, 1), 256, 0, stream>>>(d_rec.as<float>(), (int)rows.size(), nt, a,
+                                                                     it + 1, d_err.as<int>());
+        launches_now++;
+    }
+
+    // Error flags raised by the kernels: bit 4 a bounded wait that ran out
+    // (bit 8 misaligned shared memory), bit 16 the watchdog's non-finite values.
     int check_kernel_flags() {
         int h = 0;
         CUDA_TRY(cudaMemcpy(&h, d_err.p, sizeof(int), cudaMemcpyDeviceToHost));
         if (h) {
-            cudaMemset(d_err.p, 0, sizeof(int));
+            CUDA_TRY(cudaMemset(d_err.p, 0, sizeof(int)));
+            if (h & 16)
+                return fail(FWI_ERR_DIVERGED, "non-finite values in the recorded traces or the gradients "
+                                              "(device watchdog); results discarded");
             return fail(FWI_ERR_CUDA, "a kernel's shared-memory pipeline wait timed out (flag " +
                                           std::to_string(h) + "); results discarded");
         }
@@ -1448,6 +1619,7 @@ struct Engine {
             unsigned sf = (store && it % fwi_dt == 0) ? FL_STORE : 0u;
             unsigned vf = FL_INJECT | (record ? (FL_RECORD | FL_WE) : 0u);
             step(false, it, sf, vf);
+            if (record) watch(t0, it);
             if (record && snap_interval > 0 && it % snap_interval == 0) {
                 const int k = it / snap_interval;
                 for (int b = 0; b < B; b++)
@@ -1498,7 +1670,10 @@ struct Engine {
     // The binomial plan runs without state copies on the TMA mapping (the
     // other mappings and the exact adjoint copy states in and out of slots).
     bool copy_free() const { return kmap == 3 && ckpt_mode() && !exact() && slots > 0; }
-    float* buf(int k) { return k < slots ? snap(k) : d_fwd.as<float>(); }
+    float* buf(int k) { return k < slots ? snap(k) : k == slots ? d_fwd.as<float>() : d_fwd2.as<float>(); }
+    // Buffers a step can read or write: the checkpoint slots, d_fwd and, for
+    // the fused step, d_fwd2.
+    int nbufs() const { return slots + (fused() ? 2 : 1); }
     // One recompute step (stress, velocity, source injection) from the state
     // of step `it` in buffer x to the state of step it+1 in buffer y (x == y:
     // in place).  Out of place, the stress pass reads velocities and
@@ -1579,19 +1754,34 @@ struct Engine {
                 if (a.kind == Action::ADJOINT) break;
                 if (a.kind == Action::SAVE) saves.push_back({a.b, a.a});
             }
+        stall_pending = stall_next && fused();
+        stall_next = false;
         const std::string key = std::string("fwd") + (store ? "S" : "") + (ckpt ? "C" : "") +
-                                (obs ? "O" : "") + shape_key();
+                                (obs ? "O" : "") + (stall_pending ? "X" : "") + shape_key();
         FWI_TRY(run_phase(key, [&]() -> int {
             CUDA_TRY(cudaMemsetAsync(d_fwd.p, 0, (size_t)B * state * 4, stream));
             CUDA_TRY(cudaMemsetAsync(d_ws.p, 0, (size_t)B * field * 4, stream));
             int t = 0;
-            for (auto& sv : saves) {
-                const int tstate = sv.first * unit();
-                forward_steps(t, tstate, true, false);
-                t = tstate;
-                FWI_TRY(state_copy(snap(sv.second), d_fwd.as<float>()));
+            if (fused()) {
+                int cur = slots;  // d_fwd
+                for (auto& sv : saves) {
+                    const int tstate = sv.first * unit();
+                    fused_steps(t, tstate, &cur, true, false);
+                    t = tstate;
+                    FWI_TRY(state_copy(snap(sv.second), buf(cur)));
+                }
+                fused_steps(t, nt, &cur, true, store);
+                // the final state in d_fwd, as the in-place steps leave it
+                if (cur != slots) FWI_TRY(state_copy(d_fwd.as<float>(), buf(cur)));
+            } else {
+                for (auto& sv : saves) {
+                    const int tstate = sv.first * unit();
+                    forward_steps(t, tstate, true, false);
+                    t = tstate;
+                    FWI_TRY(state_copy(snap(sv.second), d_fwd.as<float>()));
+                }
+                forward_steps(t, nt, true, store);
             }
-            forward_steps(t, nt, true, store);
             if (rb_active) {
                 // the random-boundary forward, from rest, for the backward's
                 // reconstruction (the recording sweep above keeps the CPML, so
@@ -1668,12 +1858,14 @@ struct Engine {
         for (int k = 0; k < 4; k++) {
             const bool adj = k >= 2;
             if (adj && !have_adj_src) { ms[k] = 0.0; continue; }
+            if (k == 1 && fused()) { ms[k] = 0.0; continue; }  // the fused step is entry 0
             const int it = fwi_dt * (nft - 1);  // a sampled step: the gradient runs
             auto launch = [&]() {
                 // the forms of the recompute sweeps (forward) and of the adjoint
                 // sweep; source/receiver events (a separate small kernel in the
                 // TMA mapping) are left out
-                if (k == 0) pass_stress_fwd(0, itf, it, 0u);
+                if (k == 0 && fused()) fused_step(slots, slots + 1, it, 0u, 0u);
+                if (k == 0 && !fused()) pass_stress_fwd(0, itf, it, 0u);
                 if (k == 1) pass_velocity(0, itf, it, 0u);
                 if (k == 2) pass_stress_adj(ita, it, FL_GRAD);
                 if (k == 3) pass_velocity(1, ita, it, FL_WE);
@@ -1799,6 +1991,8 @@ struct Engine {
                                                        field, d_wmax.as<unsigned>());
             launches_now += 2;
         }
+        watch_array_kernel<<<num_sms * 4, 256, 0, stream>>>(d_grad.as<float>(), (size_t)B * 3 * nf, d_err.as<int>());
+        launches_now++;
         if (accumulate) {
             sum_shots_kernel<<<592, 256, 0, stream>>>(d_grad.as<float>(), d_gacc.as<float>(), 3 * nf, B, 1);
             launches_now++;
@@ -1850,6 +2044,7 @@ struct Engine {
     // slot's free one (the state stays where it is), and ADJOINT reads the
     // forward fields from whichever buffer holds them.
     int run_plan_copy_free(size_t k, int last_slot, int last_state) {
+        if (fused()) return run_plan_fused(k, last_slot, last_state);
         const int u = unit();
         std::vector<int> phys(slots);
         for (int i = 0; i < slots; i++) phys[i] = i;
@@ -1882,6 +2077,60 @@ struct Engine {
                     if (a.a < 0) {
                         CUDA_TRY(cudaMemsetAsync(buf(wb), 0, (size_t)B * state * 4, stream));
                         src = wb;
+                    } else {
+                        src = phys[a.a];
+                    }
+                    break;
+                case Action::ADJOINT: {
+                    const int t0 = a.a * fwi_dt, t1 = std::min(nt, (a.a + 1) * fwi_dt);
+                    amap_cur = &amaps_b[src];
+                    adjoint_steps(t0, t1);
+                    amap_cur = nullptr;
+                    break;
+                }
+            }
+        }
+        return FWI_OK;
+    }
+
+    // The same plan with the fused step: two working buffers (a step never
+    // writes the buffer it reads); SAVE of a state in a working buffer hands
+    // that buffer to the slot and takes the slot's free one in exchange.
+    int run_plan_fused(size_t k, int last_slot, int last_state) {
+        const int u = unit();
+        std::vector<int> phys(slots);
+        for (int i = 0; i < slots; i++) phys[i] = i;
+        int wbs[2] = {slots, slots + 1};  // the working buffers (initially d_fwd, d_fwd2)
+        int src = last_slot >= 0 ? phys[last_slot] : wbs[0];
+        if (last_slot < 0) CUDA_TRY(cudaMemsetAsync(buf(wbs[0]), 0, (size_t)B * state * 4, stream));
+        auto advance = [&](int t0, int t1) {
+            for (int it = t0; it < t1; it++) {
+                const int dst = src == wbs[0] ? wbs[1] : wbs[0];
+                fused_step(src, dst, it, 0u, FL_INJECT);
+                src = dst;
+            }
+        };
+        advance(last_state * u, (nunits() - 1) * u);
+        for (; k < plan.size(); k++) {
+            const Action& a = plan[k];
+            switch (a.kind) {
+                case Action::ADVANCE:
+                    advance(a.a * u, a.b * u);
+                    break;
+                case Action::SAVE:
+                    if (src == wbs[0] || src == wbs[1]) {
+                        int& w = src == wbs[0] ? wbs[0] : wbs[1];
+                        std::swap(phys[a.a], w);
+                        src = phys[a.a];
+                    } else {
+                        FWI_TRY(state_copy(buf(phys[a.a]), buf(src)));
+                        src = phys[a.a];
+                    }
+                    break;
+                case Action::RESTORE:
+                    if (a.a < 0) {
+                        CUDA_TRY(cudaMemsetAsync(buf(wbs[0]), 0, (size_t)B * state * 4, stream));
+                        src = wbs[0];
                     } else {
                         src = phys[a.a];
                     }
@@ -2431,9 +2680,10 @@ int fwi_psv_set_gradient_mode(fwi_psv_engine* h, int mode) {
 
 int fwi_psv_set_exec(fwi_psv_engine* h, int use_graphs, int block_x, int tile_z, int batch) {
     GUARD_ENGINE(h);
-    if ((block_x != 0 && block_x != 32 && block_x != 64 && block_x != fwi::kTileX && block_x != 256) ||
+    if ((block_x != 0 && block_x != 32 && block_x != 64 && block_x != fwi::kTileX && block_x != 256 &&
+         block_x != 512) ||
         tile_z < 0 || batch < 0)
-        return fail(FWI_ERR_INVALID, "block_x must be 0, 32, 64, 128 or 256; tile_z and batch >= 0");
+        return fail(FWI_ERR_INVALID, "block_x must be 0, 32, 64, 128, 256 or 512; tile_z and batch >= 0");
     Engine& e = h->e;
     e.use_graphs = use_graphs ? 1 : 0;
     e.bx_req = block_x;
@@ -2441,15 +2691,19 @@ int fwi_psv_set_exec(fwi_psv_engine* h, int use_graphs, int block_x, int tile_z,
     e.batch_override = batch;
     // block_x 128 (or a tile height) selects the z-march, 32 the scalar cell
     // mapping, 64 the vectorised cells, 256 the TMA-staged tiles, 0 the default
+    // (the TMA passes as two launches per forward step, the default), 512 the
+    // TMA mapping with the fused forward step (fdorder <= 8)
     const int map = (block_x == fwi::kTileX || tile_z > 0) ? 0
                     : block_x == 32                        ? 1
-                    : block_x == 256                       ? 3
+                    : block_x == 256 || block_x == 512     ? 3
                     : block_x == 64                        ? 2
                                                            : fwi::kDefaultMap;
+    e.fuse = block_x == 512;
     if (map != e.kmap) {
         if (map == 3) {
             cudaSetDevice(e.device);
             cudaError_t ce = e.tset.prepare();
+            if (ce == cudaSuccess && e.fset.prepare) ce = e.fset.prepare();
             if (ce != cudaSuccess)
                 return fail(FWI_ERR_CUDA, std::string("TMA kernels: ") + cudaGetErrorString(ce));
         }
@@ -2459,6 +2713,21 @@ int fwi_psv_set_exec(fwi_psv_engine* h, int use_graphs, int block_x, int tile_z,
     e.invalidate_batch();
     for (auto& kv : e.tilesets) kv.second->ntiles = 0;
     e.drop_graphs();
+    return FWI_OK;
+}
+
+int fwi_psv_set_wait_limit(fwi_psv_engine* h, double seconds) {
+    GUARD_ENGINE(h);
+    if (!(seconds >= 1e-6 && seconds <= 60.0)) return fail(FWI_ERR_INVALID, "wait limit must be in [1e-6, 60] s");
+    h->e.wait_ns = (unsigned long long)(seconds * 1e9);
+    h->e.invalidate_batch();  // the limit is a launch argument (captured graphs are rebuilt)
+    return FWI_OK;
+}
+
+int fwi_psv_debug_stall_next(fwi_psv_engine* h) {
+    GUARD_ENGINE(h);
+    if (!h->e.fused()) return fail(FWI_ERR_UNSUPPORTED, "the stall hook needs the fused forward step");
+    h->e.stall_next = true;
     return FWI_OK;
 }
 

@@ -99,6 +99,7 @@ struct TmaGrid {
     // CPML memories are read from (0 in place; a step out of a checkpoint
     // buffer into the working buffer reads them from the checkpoint)
     long long msrc;
+    unsigned long long wait_ns;  // limit of each bounded wait (0: kWaitNs)
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -110,6 +111,10 @@ __device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
 __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
                  : "memory");
+}
+// Raise the transaction count of the current phase without arriving.
+__device__ __forceinline__ void mbar_expect_tx_only(uint64_t* bar, unsigned bytes) {
+    asm volatile("mbarrier.expect_tx.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
 }
 __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
     uint32_t ok;
@@ -128,13 +133,16 @@ __device__ __forceinline__ unsigned long long global_ns() {
     return t;
 }
 // Bounded wait for the phase with the given parity to complete.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity) {
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity, unsigned long long limit_ns) {
     if (mbar_try_wait(bar, parity)) return true;
     const unsigned long long t0 = global_ns();
     while (true) {
         if (mbar_try_wait(bar, parity)) return true;
-        if (global_ns() - t0 > kWaitNs) return false;
+        if (global_ns() - t0 > limit_ns) return false;
     }
+}
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity) {
+    return mbar_wait_bounded(bar, parity, kWaitNs);
 }
 __device__ __forceinline__ void tma_load_3d(float* dst, const CUtensorMap* map, int x, int y, int z,
                                             uint64_t* bar) {
@@ -278,15 +286,25 @@ __device__ __forceinline__ PairCols pair_cols(const ItemDesc& D, int ix, bool st
 
 // CPML of lane l of an x-derivative pair inside an x-strip (d1 with the
 // integer-grid coefficients, d2 with the half-grid ones): its memories m1/m2
-// at m are advanced from o1/o2 and stored, and its derivatives corrected.
+// at m are advanced from o1/o2 and stored (unless `store` is false), and its
+// derivatives corrected.  The roundings are spelled out (b*o + round(a*d),
+// then d*iK + m, as the packed z-strip update does) so that every kernel
+// inlining this computes the same bits.
 __device__ __forceinline__ void cpml_x_lane(const Cpml& c, size_t m, float o1, float o2, float* __restrict__ a1,
-                                            float* __restrict__ a2, float& e1, float& e2) {
-    const float m1 = c.b * o1 + c.a * e1;
-    const float m2 = c.bh * o2 + c.ah * e2;
-    a1[m] = m1;
-    a2[m] = m2;
-    e1 = e1 * c.iK + m1;
-    e2 = e2 * c.iKh + m2;
+                                            float* __restrict__ a2, float& e1, float& e2, bool store = true) {
+    const float m1 = __fmaf_rn(c.b, o1, __fmul_rn(c.a, e1));
+    const float m2 = __fmaf_rn(c.bh, o2, __fmul_rn(c.ah, e2));
+    if (store) {
+        a1[m] = m1;
+        a2[m] = m2;
+    }
+    e1 = __fmaf_rn(e1, c.iK, m1);
+    e2 = __fmaf_rn(e2, c.iKh, m2);
+}
+// sxx on the free-surface row (forward_kernel_PSV_GPU.cu:917-927):
+// vx_x * 2 M2 (L + M2/2) / (L + M2) with L = dt lam, M2 = 2 dt mu, roundings spelled out.
+__device__ __forceinline__ float fsurf_sxx(float vx_x, float L, float M2) {
+    return __fdiv_rn(__fmul_rn(vx_x, __fmul_rn(__fmul_rn(2.f, M2), __fmaf_rn(0.5f, M2, L))), __fadd_rn(L, M2));
 }
 // Both lanes of a pair, each lane's coefficients read at the row (L1 hits):
 // the stress and adjoint passes, where holding them across rows costs spills.
@@ -488,8 +506,8 @@ __device__ __forceinline__ void stress_rows(const ItemDesc& D, const float* st, 
             if (fsurf && iz == FP) {
                 szz = make_float2(0.f, 0.f);
                 szx = make_float2(0.f, 0.f);
-                sxx.x = vx_x.x * (2.f * M2.x * (L.x + 0.5f * M2.x)) / (L.x + M2.x);
-                sxx.y = vx_x.y * (2.f * M2.y * (L.y + 0.5f * M2.y)) / (L.y + M2.y);
+                sxx.x = fsurf_sxx(vx_x.x, L.x, M2.x);
+                sxx.y = fsurf_sxx(vx_x.y, L.y, M2.y);
             }
             st2(gsxx + c, sxx, pc.on0, pc.on1);
             st2(gszx + c, szx, pc.on0, pc.on1);
@@ -705,8 +723,10 @@ __host__ __device__ constexpr size_t tma_tail_bytes() {
 }
 
 template <int FP, int STAGE_FLOATS, class Coords, class Issue, class Compute>
-__device__ __forceinline__ void tma_pipeline(int ntiles, int* err, Coords coords, Issue issue, Compute compute) {
+__device__ __forceinline__ void tma_pipeline(int ntiles, int* err, Coords coords, Issue issue, Compute compute,
+                                             unsigned long long wait_ns = 0) {
     constexpr int kTmaStages = stages_for<STAGE_FLOATS>();
+    const unsigned long long lim = wait_ns ? wait_ns : kWaitNs;
     static_assert(STAGE_FLOATS % 32 == 0, "stages are 128-byte multiples");
     // dynamic shared memory only: the stages, the tile coordinates, the barriers
     extern __shared__ __align__(128) float tma_smem[];
@@ -742,7 +762,7 @@ __device__ __forceinline__ void tma_pipeline(int ntiles, int* err, Coords coords
         if (t >= ntiles) break;
         const int s = k % kTmaStages;
         const unsigned parity = (unsigned)((k / kTmaStages) & 1);
-        const bool ok = mbar_wait_bounded(&bar[s], parity);
+        const bool ok = mbar_wait_bounded(&bar[s], parity, lim);
         if (ok) {
             // coordinates of this thread's next tile (issued already: stages >= 2)
             const int4 nx = first + (k + 1) * step < ntiles ? crd[(k + 1) % kTmaStages] : make_int4(-1, 0, 0, 0);
@@ -755,7 +775,7 @@ __device__ __forceinline__ void tma_pipeline(int ntiles, int* err, Coords coords
                 // drain the copies this CTA issued and has not consumed (bounded)
                 for (int j = k; j < k + kTmaStages; j++) {
                     const int tj = first + j * step;
-                    if (tj < ntiles) mbar_wait_bounded(&bar[j % kTmaStages], (unsigned)((j / kTmaStages) & 1));
+                    if (tj < ntiles) mbar_wait_bounded(&bar[j % kTmaStages], (unsigned)((j / kTmaStages) & 1), lim);
                 }
             }
             return;
@@ -798,7 +818,8 @@ __global__ void __launch_bounds__(kFwdThreads, 1)
         [&](int4 c, int4, const float* st) {
             stress_compute<FP>(*reinterpret_cast<const ItemDesc*>(st + G::S_DESC), g, st, c.y, c.z, it, flags, hx,
                                hz);
-        });
+        },
+        g.wait_ns);
 }
 
 template <int FP>
@@ -816,7 +837,8 @@ __global__ void __launch_bounds__(kFwdThreads, 1)
         },
         [&](int4 c, int4, const float* st) {
             velocity_compute<FP>(*reinterpret_cast<const ItemDesc*>(st + G::V_DESC), g, st, c.y, c.z, flags, hx, hz);
-        });
+        },
+        g.wait_ns);
 }
 
 // ---------------------------------------------------------------------------
@@ -1073,8 +1095,8 @@ __device__ __forceinline__ void adjoint_rows(const ItemDesc& D, const float* st,
         if (fsurf && iz == FP) {
             szz = make_float2(0.f, 0.f);
             szx = make_float2(0.f, 0.f);
-            sxx.x = vx_x.x * (2.f * M2.x * (L.x + 0.5f * M2.x)) / (L.x + M2.x);
-            sxx.y = vx_x.y * (2.f * M2.y * (L.y + 0.5f * M2.y)) / (L.y + M2.y);
+            sxx.x = fsurf_sxx(vx_x.x, L.x, M2.x);
+            sxx.y = fsurf_sxx(vx_x.y, L.y, M2.y);
         }
         st2(D.ux + c, ux, pc.on0, pc.on1);
         st2(D.uz + c, uz, pc.on0, pc.on1);
@@ -1132,7 +1154,8 @@ __global__ void __launch_bounds__(kAdjThreads, 1)
                 ga.g[5] = gr[gi + 1];
                 ga.valid = true;
             }
-        });
+        },
+        g.wait_ns);
 }
 
 // ---------------------------------------------------------------------------

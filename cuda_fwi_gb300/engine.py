@@ -98,6 +98,14 @@ class Engine:
     def set_exec(self, use_graphs=True, block_x=0, tile_z=0, batch=0):
         check(_capi.lib().fwi_psv_set_exec(self.h, int(use_graphs), block_x, tile_z, batch), "set_exec")
 
+    def set_wait_limit(self, seconds: float):
+        """Bound of every wait of the kernels on their own copies (default 2 s)."""
+        check(_capi.lib().fwi_psv_set_wait_limit(self.h, float(seconds)), "set_wait_limit")
+
+    def debug_stall_next(self):
+        """Test hook: the next forward's first fused step waits for bytes that never arrive."""
+        check(_capi.lib().fwi_psv_debug_stall_next(self.h), "debug_stall_next")
+
     def set_stream(self, stream_handle: int | None):
         check(_capi.lib().fwi_psv_set_stream(self.h, C.c_void_p(stream_handle or 0)), "set_stream")
 

@@ -386,6 +386,23 @@ int fwi_psv_multi_gradient(fwi_psv_multi* m, const double* const* obs, double* m
 int fwi_psv_multi_tuning(fwi_psv_multi* m, int group, int info[7], double ms[2]);
 int fwi_psv_multi_get_stats(fwi_psv_multi* m, fwi_psv_stats* out);
 
+/* ---- failure detection ---------------------------------------------------- */
+
+/* No counterpart in the reference (whose CUDA errors exit the process,
+ * forward_kernel_PSV_GPU.cu:19-27).  Every wait of the engine's kernels on
+ * their own asynchronous copies is bounded; when one runs out the kernel sets
+ * an error word, drains its copies (bounded) and returns, the later launches of
+ * the call return at once, and the call returns FWI_ERR_CUDA with the engine
+ * still usable.  fwi_psv_set_wait_limit sets that bound (default 2 s; 1e-6 to
+ * 60 s).  A device watchdog scans the recorded traces every 64 steps and the
+ * gradients at the end of a backward for NaN / Inf; the call then returns
+ * FWI_ERR_DIVERGED (as a residual above 1e10 does). */
+int fwi_psv_set_wait_limit(fwi_psv_engine* e, double seconds);
+/* Test hook: the next forward's first fused step makes one CTA expect more
+ * bytes than its copies deliver, so its wait runs out and the forward returns
+ * FWI_ERR_CUDA (FWI_ERR_UNSUPPORTED when the fused step is not in use). */
+int fwi_psv_debug_stall_next(fwi_psv_engine* e);
+
 /* ---- allocation-free misfit ---------------------------------------------- */
 
 /* No counterpart in the reference (whose misfit, calculate_l2_adjoint_sources,

@@ -888,9 +888,9 @@ int orc_exact_gradient(int ishot, const orc_grid* g, const double* lam, const do
  * shot: ~2.5 GB instead of 73 GB).
  * ------------------------------------------------------------------------- */
 int orc_gradient_ckpt(int ishot, const orc_grid* g, const orc_medium* m, const orc_seis* src,
-                      const double* src_signal, const orc_seis* rec, const double* obs, double* rec_signal,
-                      const orc_fwi* f, int interval, double* misfit, double* grad_lam, double* grad_mu,
-                      double* grad_rho, double* we_fwd, double* we_adj) {
+                      const double* src_signal, const orc_seis* rec, const double* obs, const double* res_in,
+                      double* rec_signal, const orc_fwi* f, int interval, double* misfit, double* grad_lam,
+                      double* grad_mu, double* grad_rho, double* we_fwd, double* we_adj) {
     int rc = check_grid(g);
     if (rc) return rc;
     if (!f || !f->fwinv || interval < 1) return -5;
@@ -936,7 +936,7 @@ int orc_gradient_ckpt(int ishot, const orc_grid* g, const orc_medium* m, const o
             size_t i = (size_t)ir * nt + it;
             double diff = rec_signal[i] - obs[i];
             J += 0.5 * g->dt * diff * diff;
-            res[i] = diff;
+            res[i] = res_in ? res_in[i] : diff;
             if (fabs(diff) > 1.0e+10) blow = 1;
         }
     }

@@ -145,14 +145,16 @@ int orc_set_threads(int n);
 /* orc_forward (storage) + orc_l2_adjoint_sources (the shot's receivers) +
  * orc_adjoint for one shot, bit-identical, with the forward wavefield kept as
  * a full state every `interval` steps and recomputed per segment.  f gives the
- * window (its storage pointers are not used); obs [nrec][nt]; writes
+ * window (its storage pointers are not used); obs [nrec][nt]; res_in, when not
+ * NULL, replaces the residual the adjoint injects ([nrec][nt], the shot's rows;
+ * the misfit still comes from obs); writes
  * rec_signal [nrec][nt] (the shot's rows), *misfit, the gradients [nfz][nfx]
  * and, when not NULL, the forward and adjoint energy [nzt][nxt].  Returns 0,
  * 1 when |syn - obs| > 1e10 somewhere, < 0 on bad arguments or no memory. */
 int orc_gradient_ckpt(int ishot, const orc_grid* g, const orc_medium* m, const orc_seis* src,
-                      const double* src_signal, const orc_seis* rec, const double* obs, double* rec_signal,
-                      const orc_fwi* f, int interval, double* misfit, double* grad_lam, double* grad_mu,
-                      double* grad_rho, double* we_fwd, double* we_adj);
+                      const double* src_signal, const orc_seis* rec, const double* obs, const double* res_in,
+                      double* rec_signal, const orc_fwi* f, int interval, double* misfit, double* grad_lam,
+                      double* grad_mu, double* grad_rho, double* we_fwd, double* we_adj);
 
 #ifdef __cplusplus
 }

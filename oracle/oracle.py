@@ -81,7 +81,7 @@ def lib():
         L.orc_set_threads.argtypes = [C.c_int]
         L.orc_set_threads.restype = C.c_int
         L.orc_gradient_ckpt.argtypes = [C.c_int, C.POINTER(Grid), C.POINTER(Medium), C.POINTER(Seis), dp,
-                                        C.POINTER(Seis), dp, dp, C.POINTER(Fwi), C.c_int, dp, dp, dp, dp,
+                                        C.POINTER(Seis), dp, dp, dp, C.POINTER(Fwi), C.c_int, dp, dp, dp, dp,
                                         dp, dp]
         L.orc_exact_gradient.argtypes = [C.c_int, C.POINTER(Grid), dp, dp, dp, C.POINTER(Seis), dp,
                                          C.POINTER(Seis), dp, dp, dp, dp, dp]
@@ -289,10 +289,12 @@ def ckpt_interval(p):
     return max(1, min(p.nt, int(round(np.sqrt(p.nt * state / frame)))))
 
 
-def gradient_ckpt(p, obs, shot=0, interval=None, lam=None, mu=None, rho=None):
+def gradient_ckpt(p, obs, shot=0, interval=None, lam=None, mu=None, rho=None, residual=None):
     """The same result as gradient() bit for bit (forward, residual, adjoint of
     one shot) with the forward wavefield recomputed from a state every
     `interval` steps instead of stored: memory for a full-size shot.
+    `residual` ([nrec][nt]) replaces the adjoint source syn - obs (the misfit
+    is still computed from obs).
     Returns (J, (grad_lam, grad_mu, grad_rho), rec, We_fwd, We_adj)."""
     ctx = _Ctx(p, lam, mu, rho)
     src, keep1 = ctx.seis(p.src_x, p.src_z, p.src_comp, p.src_shot)
@@ -307,8 +309,12 @@ def gradient_ckpt(p, obs, shot=0, interval=None, lam=None, mu=None, rho=None):
     wf, wa = np.zeros((p.nzt, p.nxt)), np.zeros((p.nzt, p.nxt))
     J = C.c_double()
     k = int(interval) if interval else ckpt_interval(p)
+    res = None if residual is None else np.ascontiguousarray(residual, np.float64)
+    if res is not None and res.shape != (p.nrec, p.nt):
+        raise ValueError("residual must be [nrec][nt]")
     rc = lib().orc_gradient_ckpt(shot, C.byref(ctx.g), C.byref(ctx.m), C.byref(src), _d(sig), C.byref(rec),
-                                 _d(ob), _d(recs), C.byref(f), k, C.byref(J), *[_d(x) for x in g], _d(wf), _d(wa))
+                                 _d(ob), _d(res) if res is not None else None, _d(recs), C.byref(f), k,
+                                 C.byref(J), *[_d(x) for x in g], _d(wf), _d(wa))
     if rc < 0:
         raise ValueError(f"orc_gradient_ckpt failed ({rc})")
     return J.value, tuple(g), recs[: p.nrec], wf, wa

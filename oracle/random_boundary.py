@@ -58,8 +58,10 @@ def frame_factor2(p):
     return f2.astype(np.float64)
 
 
-def gradient(p, obs, shot=0):
-    """(J, (grad_lam, grad_mu, grad_rho)) of the random-boundary strategy."""
+def gradient(p, obs, shot=0, residual=None):
+    """(J, (grad_lam, grad_mu, grad_rho)) of the random-boundary strategy.
+    `residual` ([nrec][nt]) replaces the adjoint source syn - obs (J still
+    comes from obs)."""
     f2 = frame_factor2(p)
     mzx, rzp, rxp = O.average(p.lam, p.mu, p.rho)
     ident = {k: (np.ones_like(v) if k in ("K", "K_half") else np.zeros_like(v)) for k, v in p.cpml.items()}
@@ -68,5 +70,7 @@ def gradient(p, obs, shot=0):
                    averaged=(mzx * f2[:-1, :-1], rzp, rxp))
     rows = O.shot_rows(p, shot)
     J, res, _ = O.residual(O.forward(p, shot)["rec"], obs, p.dt, rows)
+    if residual is not None:
+        res = np.ascontiguousarray(residual, np.float64)
     ad = O.adjoint(p, shot, res, fw["store"])
     return J, (ad["grad_lam"], ad["grad_mu"], ad["grad_rho"])

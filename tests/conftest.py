@@ -33,3 +33,14 @@ def gpu():
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device")
     return 0
+
+
+def engine_residual(rec, obs, rows):
+    """The engine's adjoint source for traces `rec` (its FP32 seismograms): FP32
+    synthetics minus FP32 observed data, differenced in FP64 and rounded to
+    FP32 (residual_kernel); zero outside `rows`."""
+    import numpy as np
+    r = np.zeros_like(np.asarray(obs, np.float64))
+    o32 = np.asarray(obs, np.float64)[rows].astype(np.float32).astype(np.float64)
+    r[rows] = (np.asarray(rec, np.float64)[rows] - o32).astype(np.float32)
+    return r

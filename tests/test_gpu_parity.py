@@ -19,8 +19,9 @@ SEIS_TOL = 1e-5
 GRAD_TOL = 1e-4
 
 
-# block_x of set_exec: 64 = vectorised cells, 256 = TMA-staged tiles (the default)
-MAPPINGS = [64, 256]
+# block_x of set_exec: 64 = vectorised cells, 256 = TMA-staged tiles with two passes per
+# forward step (the default mapping), 512 = TMA-staged tiles with the fused forward step
+MAPPINGS = [64, 256, 512]
 
 
 @pytest.mark.parametrize("bx", MAPPINGS)
