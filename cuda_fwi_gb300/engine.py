@@ -98,6 +98,17 @@ class Engine:
     def set_exec(self, use_graphs=True, block_x=0, tile_z=0, batch=0):
         check(_capi.lib().fwi_psv_set_exec(self.h, int(use_graphs), block_x, tile_z, batch), "set_exec")
 
+    def set_snapshots(self, interval: int, which: int = 4):
+        """Keep field `which` (0 vx .. 4 szz) of every batch slot every `interval` steps
+        of the recording sweep (the reference's vz_snap files hold szz: which = 4)."""
+        check(_capi.lib().fwi_psv_set_snapshots(self.h, int(interval), int(which)), "set_snapshots")
+
+    def snapshot(self, slot: int, k: int):
+        """Snapshot k (step k * interval) of batch slot `slot` of the last forward, [nzt][nxt]."""
+        out = np.zeros((self.p.nzt, self.p.nxt))
+        check(_capi.lib().fwi_psv_snapshot(self.h, int(slot), int(k), pd(out)), "snapshot")
+        return out
+
     def set_wait_limit(self, seconds: float):
         """Bound of every wait of the kernels on their own copies (default 2 s)."""
         check(_capi.lib().fwi_psv_set_wait_limit(self.h, float(seconds)), "set_wait_limit")

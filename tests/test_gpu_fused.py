@@ -42,13 +42,13 @@ def _run(p, obs, bx, strategy, snapshots=0, snap_interval=0):
             eng.set_snapshots(snap_interval)
         shots = list(range(p.nshots))
         rec, mis = eng.forward(shots, obs, keep=True)
+        launches = eng.stats()["launches"]  # of the forward sweep
         w = eng.wavefield(0, p.nshots - 1)
         ws, _ = eng.energy(p.nshots - 1)
         snaps = eng.snapshot(p.nshots - 1, 1) if snap_interval else None
         g = eng.backward()
         _, wr = eng.energy(0)
-        st = eng.stats()
-    return dict(rec=rec, mis=mis, w=w, ws=ws, g=g, wr=wr, snaps=snaps, launches=st["launches"])
+    return dict(rec=rec, mis=mis, w=w, ws=ws, g=g, wr=wr, snaps=snaps, launches=launches)
 
 
 def _assert_equal(a, b):
