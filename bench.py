@@ -77,13 +77,14 @@ def peaks():
         return HBM_FALLBACK_GBS, "fallback"
 
 
-def workload(args, setup=None):
+def workload(args, setup=None, world=1):
     """(true, synthetic) problems of the workload; `setup` replaces the engine
-    library's setup helpers (the reference arm passes the oracle's)."""
+    library's setup helpers (the reference arm passes the oracle's).  With
+    `world` ranks the survey has args.shots shots per rank (weak scaling)."""
     from cuda_fwi_gb300 import problem as P
     P.use_setup_helpers(setup)
-    true = P.config3(True, nshots=args.shots)
-    syn = P.config3(False, nshots=args.shots)
+    true = P.config3(True, nshots=args.shots * world)
+    syn = P.config3(False, nshots=args.shots * world)
     if args.nt:
         from dataclasses import replace
         for name in ("true", "syn"):
@@ -265,7 +266,7 @@ def main():
     if args.impl == "reference":
         return run_reference(args, rank)
 
-    true, syn = workload(args)
+    true, syn = workload(args, world=world)
     # CPU baseline first: its spawn pool starts before any CUDA call.
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -284,7 +285,11 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
 
-    shots = list(range(args.shots))
+    # this rank's shots: every rank takes args.shots of the survey's args.shots * world
+    # (cuda_fwi_gb300.distributed.shard_shots, the sharding its gloo test covers)
+    from cuda_fwi_gb300 import distributed as D
+    all_shots = list(range(args.shots * world))
+    shots = D.shard_shots(all_shots, rank, world)
     with Engine(true, device=local) as e:
         e.set_exec(use_graphs=True)
         obs, _ = e.forward(shots)
@@ -301,12 +306,13 @@ def main():
         eng.gradient(shots, None, resident=True, want=False)
 
     def step_e2e():
-        # public API with host buffers: FP64 observed data in, summed FP64 gradient out
-        g, mis = eng.gradient(shots, obs)
-        if dist is not None:
-            t = torch.from_numpy(np.stack(g)).cuda(local)
-            dist.all_reduce(t)
-            t.cpu()
+        # public API with host buffers: FP64 observed data in, summed FP64 gradient out;
+        # with several ranks, the survey's gradient: this rank's shots, then one all-reduce
+        if dist is None:
+            g, mis = eng.gradient(shots, obs)
+            return mis
+        g, mis = D.distributed_gradient(lambda s: eng.gradient(s, obs), all_shots, len(all_shots), rank, world,
+                                        device=f"cuda:{local}")
         return mis
 
     # warm-up (captures the CUDA graphs; the first call uploads the observed data)
