@@ -63,7 +63,7 @@ class Layout(C.Structure):
 class FwiOpts(C.Structure):
     _fields_ = [("max_iter", C.c_int), ("max_error", C.c_double), ("step_length", C.c_double),
                 ("order", C.c_int), ("trial_misfit", C.c_int), ("precondition", C.c_int),
-                ("true_lam", dp), ("true_mu", dp), ("true_rho", dp)]
+                ("true_lam", dp), ("true_mu", dp), ("true_rho", dp), ("restart_step", C.c_double)]
 
 
 class FwiIter(C.Structure):

@@ -342,7 +342,7 @@ extern "C" int fwi_psv_fwi_run(fwi_psv_engine* e, const fwi_psv_fwi_opts* o, int
                                int* done) {
     if (!e || !o || nshots < 1 || !ids || !obs || !lam || !mu || !rho || !log)
         return fwi::fail(FWI_ERR_INVALID, "bad arguments to fwi_psv_fwi_run");
-    if (o->max_iter < 0 || !(o->step_length > 0) ||
+    if (o->max_iter < 0 || !(o->step_length > 0) || !(o->restart_step >= 0.0) ||
         (o->order != FWI_ORDER_SUMMED && o->order != FWI_ORDER_PER_SHOT) ||
         (o->trial_misfit != FWI_TRIAL_SUM && o->trial_misfit != FWI_TRIAL_LAST_SHOT))
         return fwi::fail(FWI_ERR_INVALID, "bad FWI options");
@@ -394,6 +394,12 @@ extern "C" int fwi_psv_fwi_run(fwi_psv_engine* e, const fwi_psv_fwi_opts* o, int
             double opt = 0.0;
             int trials = 0, status = 0;
             OPT_TRY(fwi_psv_step_search(step, L0, driver_trial, &d, &opt, &trials, &status));
+            if (status == 1 && o->restart_step > 0.0) {
+                // opt-in continuation: one more search on the same gradient from restart_step
+                int more = 0;
+                OPT_TRY(fwi_psv_step_search(o->restart_step, L0, driver_trial, &d, &opt, &more, &status));
+                trials += more;
+            }
             rec.trials = trials;
             rec.status = status;
             if (status == 1) {

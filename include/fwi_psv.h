@@ -314,11 +314,16 @@ typedef struct fwi_psv_fwi_opts {
     int trial_misfit;      /* FWI_TRIAL_* */
     int precondition;      /* energy-weight preconditioning (the reference: 1) */
     const double *true_lam, *true_mu, *true_rho; /* optional [nzt][nxt]: model error per iteration */
+    double restart_step;   /* no counterpart in the reference, which exits when a search finds no
+                            * step that lowers the misfit: > 0 retries such a search once, on the
+                            * same gradient, from this step-length estimate (e.g. the initial one,
+                            * after the searches' starting steps have shrunk); 0 stops there, as
+                            * the reference would (status 1) */
 } fwi_psv_fwi_opts;
 typedef struct fwi_psv_fwi_iter {
     double misfit;         /* summed shot misfit at the model the gradient was taken at */
     double step_length;    /* step of the parabolic fit (0 when the search failed) */
-    int trials;            /* trial forward sweeps (over all shots) of the search */
+    int trials;            /* trial forward sweeps (over all shots) of the search (and its retry) */
     int status;            /* 0; 1 no step reduced the misfit (model kept); 2 no bracketing third step */
     double model_error;    /* ||m - m_true|| / ||m_true|| over lam, mu, rho (each relative), or -1 */
     double seconds;        /* wall time of the iteration */

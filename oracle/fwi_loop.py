@@ -117,7 +117,7 @@ def misfits(p, obs, shots, lam, mu, rho):
     return [O.misfit(p, obs, s, lam, mu, rho) for s in shots]
 
 
-def fwi_loop(p, obs, shots, iters, step0=0.01, precondition=True, trial="sum", order="summed"):
+def fwi_loop(p, obs, shots, iters, step0=0.01, precondition=True, trial="sum", order="summed", restart_step=0.0):
     """The inversion loop.  order "summed": one update per iteration from the
     shot-summed gradient; "per_shot": the reference's order
     (fd_wave_model.cu:777-955), one gradient, step search and update per shot
@@ -128,7 +128,9 @@ def fwi_loop(p, obs, shots, iters, step0=0.01, precondition=True, trial="sum", o
     gradient's own misfit.  The material constants C (medium_average) are taken
     once per iteration; the staggered averages that each gradient and trial
     forward use come from the model it runs on.  A failed search (status 1)
-    stops the loop with the model unchanged.  Returns (lam, mu, rho, log) with
+    stops the loop with the model unchanged, unless restart_step > 0: then the
+    search is run once more on the same gradient from restart_step (the
+    engine's opt-in continuation; trials add up).  Returns (lam, mu, rho, log) with
     one entry dict(misfit, step_length, trials, status) per update."""
     lam, mu, rho = p.lam.copy(), p.mu.copy(), p.rho.copy()
     step = step0
@@ -160,6 +162,9 @@ def fwi_loop(p, obs, shots, iters, step0=0.01, precondition=True, trial="sum", o
                 return mis[-1] if trial == "last" else sum(mis)
 
             opt, calls, status, _ = step_search(step, L0, trial_fn)
+            if status == 1 and restart_step > 0:
+                opt, more, status, _ = step_search(restart_step, L0, trial_fn)
+                calls += more
             log.append(dict(misfit=L0, step_length=opt if status != 1 else 0.0, trials=calls, status=status))
             if status == 1:
                 return lam, mu, rho, log

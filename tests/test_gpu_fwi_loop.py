@@ -110,3 +110,21 @@ def test_fwi_loop_per_shot_order_follows_restatement(trial):
         assert a["step_length"] == pytest.approx(b["step_length"], rel=1e-3)
     for got, want, start in ((lam, lam_r, p.lam), (mu, mu_r, p.mu), (rho, rho_r, p.rho)):
         assert rel_l2(got - start, want - start) <= 1e-3
+
+
+def test_failed_search_retry_follows_restatement():
+    """The opt-in continuation (restart_step > 0): a search that finds no step
+    lowering the misfit is run once more on the same gradient from restart_step
+    before the loop stops.  In this per-shot, last-shot-trial case both searches
+    fail (14 trial sweeps in all); the engine's log and model equal the
+    restatement's (the model unchanged)."""
+    p, t, obs = _case()
+    lam_r, mu_r, rho_r, log_r = FL.fwi_loop(p, obs, [0, 1], iters=2, step0=0.01, order="per_shot", trial="last",
+                                            restart_step=0.05)
+    with Engine(p) as eng:
+        eng.set_strategy("binomial", snapshots=8)
+        (lam, mu, rho), log = eng.fwi_run([0, 1], obs, max_iter=2, step_length=0.01, order="per_shot",
+                                          trial="last", restart_step=0.05)
+    assert [(a["trials"], a["status"]) for a in log] == [(b["trials"], b["status"]) for b in log_r] == [(14, 1)]
+    assert log[0]["misfit"] == pytest.approx(log_r[0]["misfit"], rel=1e-4)
+    assert np.array_equal(lam, p.lam) and np.array_equal(mu, p.mu) and np.array_equal(rho, p.rho)
