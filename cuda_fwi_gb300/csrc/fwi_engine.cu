@@ -726,7 +726,7 @@ struct Engine {
     FusedGrid fgrid{};
     int grid_fused = 1;
     unsigned long long wait_ns = kWaitNs;  // limit of the kernels' bounded waits
-    bool stall_next = false, stall_pending = false;  // test hook: one fused step whose wait runs out
+    bool stall_next = false, stall_pending = false;  // test hook: one forward step whose wait runs out
     bool zero_mu = false;  // some interior cell has mu == 0 (exact mode unsupported)
     // energy-weight preconditioning of each shot's gradient (fd_wave_model.cu:1004-1052)
     bool pre_on = false;
@@ -1457,8 +1457,14 @@ struct Engine {
 
     // Forward stress and velocity passes of one state buffer (0 fwd, 1 adj, 2 state n+1).
     void pass_stress_fwd(int w, const ItemDesc* items, int it, unsigned flags) {
-        if (kmap == 3) tset.stress(dim3(grid_tma), stream, smaps[w], items, tgrid, it, flags, d_err.as<int>());
-        else ks.stress_f(dim3(grid_sf), stream, items, d_tiles_p, ntiles, it, flags, d_err.as<int>());
+        if (kmap == 3) {
+            TmaGrid g = tgrid;
+            g.stall = stall_pending ? 1 : 0;
+            stall_pending = false;
+            tset.stress(dim3(grid_tma), stream, smaps[w], items, g, it, flags, d_err.as<int>());
+        } else {
+            ks.stress_f(dim3(grid_sf), stream, items, d_tiles_p, ntiles, it, flags, d_err.as<int>());
+        }
     }
     void pass_velocity(int w, const ItemDesc* items, int it, unsigned flags) {
         if (kmap == 3) {
@@ -1754,7 +1760,7 @@ struct Engine {
                 if (a.kind == Action::ADJOINT) break;
                 if (a.kind == Action::SAVE) saves.push_back({a.b, a.a});
             }
-        stall_pending = stall_next && fused();
+        stall_pending = stall_next && (fused() || (kmap == 3 && !exact()));
         stall_next = false;
         const std::string key = std::string("fwd") + (store ? "S" : "") + (ckpt ? "C" : "") +
                                 (obs ? "O" : "") + (stall_pending ? "X" : "") + shape_key();
@@ -2726,7 +2732,8 @@ int fwi_psv_set_wait_limit(fwi_psv_engine* h, double seconds) {
 
 int fwi_psv_debug_stall_next(fwi_psv_engine* h) {
     GUARD_ENGINE(h);
-    if (!h->e.fused()) return fail(FWI_ERR_UNSUPPORTED, "the stall hook needs the fused forward step");
+    if (!h->e.fused() && (h->e.kmap != 3 || h->e.exact()))
+        return fail(FWI_ERR_UNSUPPORTED, "the stall hook needs a TMA forward step (block_x 256 or 512, reference gradient)");
     h->e.stall_next = true;
     return FWI_OK;
 }

@@ -92,7 +92,8 @@ struct VelMaps {
 // [gxl, gxh] x [gzl, gzh]: the gradient window when it is sampled at unit
 // intervals (empty otherwise).
 struct TmaGrid {
-    int nb, ntz, ntiles, pad;
+    int nb, ntz, ntiles;
+    int stall;  // test hook: CTA 0's first stage expects 16 bytes its copies do not deliver
     int cxl, cxh, czl, czh;
     int gxl, gxh, gzl, gzh;
     // forward passes: offset (floats) from the written state to the state the
@@ -253,8 +254,8 @@ struct RowPairs {
 // The warp's 64 columns x kPairRows rows lie inside the grid's plain-stencil
 // cells and no storage sample is taken: it runs the branch-free row loop.
 // The decision is the same for every thread of the warp.
-__device__ __forceinline__ bool interior_warp(const TmaGrid& g, int x0, int z0, unsigned flags) {
-    const int w = threadIdx.x >> 5;
+__device__ __forceinline__ bool interior_warp(const TmaGrid& g, int x0, int z0, unsigned flags, int lt) {
+    const int w = lt >> 5;
     const int wx0 = x0 + (w & 1) * 64, wz0 = z0 + (w >> 1) * 2;
     return !(flags & FL_STORE) && wx0 >= g.cxl && wx0 + 63 <= g.cxh && wz0 >= g.czl && wz0 + 1 <= g.czh;
 }
@@ -373,12 +374,12 @@ __device__ __forceinline__ void stress_issue(const StressMaps& m, const ItemDesc
 template <int FP, bool INTERIOR>
 __device__ __forceinline__ void stress_rows(const ItemDesc& D, const float* st, int x0, int z0, int it,
                                             unsigned flags, const float2 (&hx)[FP], const float2 (&hz)[FP],
-                                            long long msrc) {
+                                            long long msrc, int lt) {
     using G = TmaGeom<FP>;
     constexpr int R = kPairRows;
     constexpr int W = R + 2 * FP - 1;
-    const int cp = (threadIdx.x & (kTmaTX / 2 - 1)) * 2;  // tile column of the pair
-    const int r0 = (threadIdx.x / (kTmaTX / 2)) * R;
+    const int cp = (lt & (kTmaTX / 2 - 1)) * 2;  // tile column of the pair
+    const int r0 = (lt / (kTmaTX / 2)) * R;
     const int ix = x0 + cp;
     PairCols pc = {true, true, {-1, -1}};
     if constexpr (!INTERIOR) {
@@ -524,9 +525,9 @@ __device__ __forceinline__ void stress_rows(const ItemDesc& D, const float* st, 
 template <int FP>
 __device__ __forceinline__ void stress_compute(const ItemDesc& D, const TmaGrid& g, const float* st, int x0, int z0,
                                                int it, unsigned flags, const float2 (&hx)[FP],
-                                               const float2 (&hz)[FP]) {
-    if (interior_warp(g, x0, z0, flags)) stress_rows<FP, true>(D, st, x0, z0, it, flags, hx, hz, g.msrc);
-    else stress_rows<FP, false>(D, st, x0, z0, it, flags, hx, hz, g.msrc);
+                                               const float2 (&hz)[FP], int lt) {
+    if (interior_warp(g, x0, z0, flags, lt)) stress_rows<FP, true>(D, st, x0, z0, it, flags, hx, hz, g.msrc, lt);
+    else stress_rows<FP, false>(D, st, x0, z0, it, flags, hx, hz, g.msrc, lt);
 }
 
 // ---------------------------------------------------------------------------
@@ -575,12 +576,13 @@ __device__ __forceinline__ void velocity_issue2(const VelMaps& ms, const VelMaps
 
 template <int FP, bool INTERIOR>
 __device__ __forceinline__ void velocity_rows(const ItemDesc& D, const float* st, int x0, int z0, unsigned flags,
-                                              const float2 (&hx)[FP], const float2 (&hz)[FP], long long msrc) {
+                                              const float2 (&hx)[FP], const float2 (&hz)[FP], long long msrc,
+                                              int lt) {
     using G = TmaGeom<FP>;
     constexpr int R = kPairRows;
     constexpr int W = R + 2 * FP - 1;
-    const int cp = (threadIdx.x & (kTmaTX / 2 - 1)) * 2;
-    const int r0 = (threadIdx.x / (kTmaTX / 2)) * R;
+    const int cp = (lt & (kTmaTX / 2 - 1)) * 2;
+    const int r0 = (lt / (kTmaTX / 2)) * R;
     const int ix = x0 + cp;
     PairCols pc = {true, true, {-1, -1}};
     if constexpr (!INTERIOR) {
@@ -692,9 +694,9 @@ __device__ __forceinline__ void velocity_rows(const ItemDesc& D, const float* st
 template <int FP>
 __device__ __forceinline__ void velocity_compute(const ItemDesc& D, const TmaGrid& g, const float* st, int x0,
                                                  int z0, unsigned flags, const float2 (&hx)[FP],
-                                                 const float2 (&hz)[FP]) {
-    if (interior_warp(g, x0, z0, flags)) velocity_rows<FP, true>(D, st, x0, z0, flags, hx, hz, g.msrc);
-    else velocity_rows<FP, false>(D, st, x0, z0, flags, hx, hz, g.msrc);
+                                                 const float2 (&hz)[FP], int lt) {
+    if (interior_warp(g, x0, z0, flags, lt)) velocity_rows<FP, true>(D, st, x0, z0, flags, hx, hz, g.msrc, lt);
+    else velocity_rows<FP, false>(D, st, x0, z0, flags, hx, hz, g.msrc, lt);
 }
 
 // Stencil weights of a launch (every slot of a launch has the same grid),
@@ -790,15 +792,124 @@ __device__ __forceinline__ void tma_pipeline(int ntiles, int* err, Coords coords
     }
 }
 
+// Warp-released variant of the pipeline, for the forward passes (whose tiles
+// read nothing another tile of the launch writes, and whose warps need no
+// data of one another): there is no CTA barrier per tile.  Each warp, once
+// done with a stage, counts itself on the stage's release counter, and the
+// warp that completes the count refills the stage with the CTA's tile S ahead.
+// A warp may so run up to S-1 tiles ahead of the slowest one, instead of every
+// warp of a tile waiting at a barrier for the warps holding its CPML strips.
+// COMPUTE(tile, stage_ptr, k) gets the CTA's tile count k as well, from which
+// the passes rotate the warps' roles: warp w does the rows and columns of
+// warp (w + k) mod nwarps of the plain mapping, so the strip work of edge
+// tiles falls on every warp in turn rather than on the same ones.
+// A wait that gives up sets bit 2 of the error word and the abort word; the
+// other warps leave at their next tile (or when their own wait gives up, the
+// released count of a stage never completing), and after a CTA barrier one
+// thread waits, bounded, for the last copy issued into each stage.
+template <int STAGES>
+__host__ __device__ constexpr size_t tma_tail_bytes_warps() {
+    return STAGES * (sizeof(int4) + sizeof(uint64_t) + 2 * sizeof(unsigned)) + 16;
+}
+
+__device__ __forceinline__ unsigned atom_add_acq_rel_cta(unsigned* p, unsigned v) {
+    unsigned old;
+    asm volatile("atom.acq_rel.cta.shared::cta.add.u32 %0, [%1], %2;"
+                 : "=r"(old)
+                 : "r"(smem_u32(p)), "r"(v)
+                 : "memory");
+    return old;
+}
+
+template <int FP, int STAGE_FLOATS, class Coords, class Issue, class Compute>
+__device__ __forceinline__ void tma_pipeline_warps(int ntiles, int* err, Coords coords, Issue issue,
+                                                   Compute compute, unsigned long long wait_ns = 0,
+                                                   int stall = 0) {
+    constexpr int S = stages_for<STAGE_FLOATS>();
+    const unsigned long long lim = wait_ns ? wait_ns : kWaitNs;
+    static_assert(STAGE_FLOATS % 32 == 0, "stages are 128-byte multiples");
+    extern __shared__ __align__(128) float tma_smem[];
+    int4* crd = reinterpret_cast<int4*>(tma_smem + S * STAGE_FLOATS);
+    uint64_t* bar = reinterpret_cast<uint64_t*>(crd + S);
+    unsigned* released = reinterpret_cast<unsigned*>(bar + S);  // running count of warps done per stage
+    unsigned* issued = released + S;                            // copies issued into each stage
+    volatile int* abort = reinterpret_cast<volatile int*>(issued + S);
+    const int tid = threadIdx.x, lane = tid & 31;
+    const unsigned nwarps = blockDim.x >> 5;
+    if (__syncthreads_or(*(volatile int*)err != 0)) return;
+    if (smem_u32(tma_smem) & 127u) {
+        if (tid == 0) atomicOr(err, 8);
+        return;
+    }
+    const int first = blockIdx.x, step = gridDim.x;
+    auto issue_tile = [&](int t, int s) {
+        int b, x0, z0;
+        coords(t, &b, &x0, &z0);
+        crd[s] = make_int4(b, x0, z0, 0);
+        issued[s] += 1u;
+        issue(b, x0, z0, tma_smem + s * STAGE_FLOATS, &bar[s]);
+    };
+    if (tid == 0) {
+        for (int s = 0; s < S; s++) {
+            mbar_init(&bar[s], 1);
+            released[s] = 0u;
+            issued[s] = 0u;
+        }
+        *abort = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        if (stall && blockIdx.x == 0) mbar_expect_tx_only(&bar[0], 16u);
+        for (int s = 0; s < S; s++) {
+            const int t = first + s * step;
+            if (t < ntiles) issue_tile(t, s);
+        }
+    }
+    __syncthreads();
+    for (int k = 0;; k++) {
+        const int t = first + k * step;
+        if (t >= ntiles || __any_sync(0xffffffffu, *abort != 0)) break;
+        const int s = k % S;
+        if (!__all_sync(0xffffffffu, mbar_wait_bounded(&bar[s], (unsigned)((k / S) & 1), lim))) {
+            if (lane == 0) {
+                *abort = 1;
+                atomicOr(err, 4);
+            }
+            break;
+        }
+        compute(crd[s], tma_smem + s * STAGE_FLOATS, k);
+        // the warp's reads of stage s are done; the release (acq_rel atomic)
+        // orders them before the refill's async-proxy writes
+        __syncwarp();
+        if (lane == 0 && (atom_add_acq_rel_cta(&released[s], 1u) + 1u) % nwarps == 0u) {
+            const int tn = first + (k + S) * step;
+            if (tn < ntiles) {
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                issue_tile(tn, s);
+            }
+        }
+    }
+    __syncthreads();
+    if (tid == 0 && *abort) {
+        for (int s = 0; s < S; s++)
+            if (issued[s]) mbar_wait_bounded(&bar[s], (issued[s] - 1u) & 1u, lim);
+    }
+}
+
+// Logical thread of the plain forward mapping that thread threadIdx.x plays
+// in the CTA's k-th tile (warp rotation, above).
+__device__ __forceinline__ int rotated_thread(int k) {
+    static_assert((kFwdThreads & (kFwdThreads - 1)) == 0, "the rotation wraps a power of two");
+    return (int)((threadIdx.x + ((unsigned)k << 5)) & (kFwdThreads - 1));
+}
+
 template <int FP>
 constexpr size_t stress_tma_smem() {
     constexpr int S = stages_for<TmaGeom<FP>::S_STAGE>();
-    return sizeof(float) * S * TmaGeom<FP>::S_STAGE + tma_tail_bytes<S>();
+    return sizeof(float) * S * TmaGeom<FP>::S_STAGE + tma_tail_bytes_warps<S>();
 }
 template <int FP>
 constexpr size_t velocity_tma_smem() {
     constexpr int S = stages_for<TmaGeom<FP>::V_STAGE>();
-    return sizeof(float) * S * TmaGeom<FP>::V_STAGE + tma_tail_bytes<S>();
+    return sizeof(float) * S * TmaGeom<FP>::V_STAGE + tma_tail_bytes_warps<S>();
 }
 static_assert(stress_tma_smem<4>() <= 232448 && velocity_tma_smem<4>() <= 232448, "shared memory per CTA");
 static_assert(stress_tma_smem<6>() <= 232448 && velocity_tma_smem<6>() <= 232448, "shared memory per CTA");
@@ -810,16 +921,16 @@ __global__ void __launch_bounds__(kFwdThreads, 1)
     using G = TmaGeom<FP>;
     float2 hx[FP], hz[FP];
     load_weights<FP>(items, hx, hz);
-    tma_pipeline<FP, G::S_STAGE>(
+    tma_pipeline_warps<FP, G::S_STAGE>(
         g.ntiles, err, [&](int t, int* b, int* x0, int* z0) { tile_coords(g, t, b, x0, z0, FP, kTmaTZ); },
         [&](int b, int x0, int z0, float* st, uint64_t* bar) {
             stress_issue<FP>(maps, items + b, b, x0, z0, st, bar);
         },
-        [&](int4 c, int4, const float* st) {
+        [&](int4 c, const float* st, int k) {
             stress_compute<FP>(*reinterpret_cast<const ItemDesc*>(st + G::S_DESC), g, st, c.y, c.z, it, flags, hx,
-                               hz);
+                               hz, rotated_thread(k));
         },
-        g.wait_ns);
+        g.wait_ns, g.stall);
 }
 
 template <int FP>
@@ -830,13 +941,14 @@ __global__ void __launch_bounds__(kFwdThreads, 1)
     const bool we = (flags & FL_WE) != 0;
     float2 hx[FP], hz[FP];
     load_weights<FP>(items, hx, hz);
-    tma_pipeline<FP, G::V_STAGE>(
+    tma_pipeline_warps<FP, G::V_STAGE>(
         g.ntiles, err, [&](int t, int* b, int* x0, int* z0) { tile_coords(g, t, b, x0, z0, FP, kTmaTZ); },
         [&](int b, int x0, int z0, float* st, uint64_t* bar) {
             velocity_issue<FP>(maps, items + b, b, x0, z0, st, bar, we);
         },
-        [&](int4 c, int4, const float* st) {
-            velocity_compute<FP>(*reinterpret_cast<const ItemDesc*>(st + G::V_DESC), g, st, c.y, c.z, flags, hx, hz);
+        [&](int4 c, const float* st, int k) {
+            velocity_compute<FP>(*reinterpret_cast<const ItemDesc*>(st + G::V_DESC), g, st, c.y, c.z, flags, hx, hz,
+                                 rotated_thread(k));
         },
         g.wait_ns);
 }
@@ -1220,7 +1332,7 @@ __global__ void __launch_bounds__(kFwdThreads, 1)
                             unsigned flags, long long msrc, int* err) {
     const MultiMaps* maps = mx;
     using G = TmaGeom<FP>;
-    tma_pipeline<FP, G::S_STAGE>(
+    tma_pipeline_warps<FP, G::S_STAGE>(
         ntiles, err,
         [&](int t, int* b, int* x0, int* z0) {
             const Tile T = tiles[t];
@@ -1231,13 +1343,13 @@ __global__ void __launch_bounds__(kFwdThreads, 1)
         [&](int b, int x0, int z0, float* st, uint64_t* bar) {
             stress_issue<FP>(maps[b].sf, items + b, 0, x0, z0, st, bar);
         },
-        [&](int4 c, int4, const float* st) {
+        [&](int4 c, const float* st, int k) {
             const ItemDesc& D = *reinterpret_cast<const ItemDesc*>(st + G::S_DESC);
             float2 hx[FP], hz[FP];
             staged_weights<FP>(D, hx, hz);
             TmaGrid gg = model_ranges(D);
             gg.msrc = msrc;
-            stress_compute<FP>(D, gg, st, c.y, c.z, it, flags, hx, hz);
+            stress_compute<FP>(D, gg, st, c.y, c.z, it, flags, hx, hz, rotated_thread(k));
         });
 }
 
@@ -1248,7 +1360,7 @@ __global__ void __launch_bounds__(kFwdThreads, 1)
                               unsigned flags, int adj, long long msrc, int* err) {
     using G = TmaGeom<FP>;
     const bool we = (flags & FL_WE) != 0;
-    tma_pipeline<FP, G::V_STAGE>(
+    tma_pipeline_warps<FP, G::V_STAGE>(
         ntiles, err,
         [&](int t, int* b, int* x0, int* z0) {
             const Tile T = tiles[t];
@@ -1260,13 +1372,13 @@ __global__ void __launch_bounds__(kFwdThreads, 1)
             if (adj) velocity_issue<FP>(mx[b].va, items + b, 0, x0, z0, st, bar, we);
             else velocity_issue2<FP>(my[b].vf, mx[b].vf, items + b, 0, x0, z0, st, bar, we);
         },
-        [&](int4 c, int4, const float* st) {
+        [&](int4 c, const float* st, int k) {
             const ItemDesc& D = *reinterpret_cast<const ItemDesc*>(st + G::V_DESC);
             float2 hx[FP], hz[FP];
             staged_weights<FP>(D, hx, hz);
             TmaGrid gg = model_ranges(D);
             gg.msrc = msrc;
-            velocity_compute<FP>(D, gg, st, c.y, c.z, flags, hx, hz);
+            velocity_compute<FP>(D, gg, st, c.y, c.z, flags, hx, hz, rotated_thread(k));
         });
 }
 

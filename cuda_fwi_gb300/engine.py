@@ -114,7 +114,7 @@ class Engine:
         check(_capi.lib().fwi_psv_set_wait_limit(self.h, float(seconds)), "set_wait_limit")
 
     def debug_stall_next(self):
-        """Test hook: the next forward's first fused step waits for bytes that never arrive."""
+        """Test hook: the next forward's first TMA-staged step waits for bytes that never arrive."""
         check(_capi.lib().fwi_psv_debug_stall_next(self.h), "debug_stall_next")
 
     def set_stream(self, stream_handle: int | None):

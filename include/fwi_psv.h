@@ -403,9 +403,10 @@ int fwi_psv_multi_get_stats(fwi_psv_multi* m, fwi_psv_stats* out);
  * gradients at the end of a backward for NaN / Inf; the call then returns
  * FWI_ERR_DIVERGED (as a residual above 1e10 does). */
 int fwi_psv_set_wait_limit(fwi_psv_engine* e, double seconds);
-/* Test hook: the next forward's first fused step makes one CTA expect more
- * bytes than its copies deliver, so its wait runs out and the forward returns
- * FWI_ERR_CUDA (FWI_ERR_UNSUPPORTED when the fused step is not in use). */
+/* Test hook: the next forward's first TMA-staged step (the fused step, or the
+ * stress pass of the two-pass step) makes one CTA expect more bytes than its
+ * copies deliver, so its wait runs out and the forward returns FWI_ERR_CUDA
+ * (FWI_ERR_UNSUPPORTED on the other mappings and with the exact adjoint). */
 int fwi_psv_debug_stall_next(fwi_psv_engine* e);
 
 /* ---- allocation-free misfit ---------------------------------------------- */

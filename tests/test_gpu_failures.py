@@ -1,11 +1,12 @@
 """Failure detection on the GPU, in the forms that leave the GPU usable.
 
 * A bounded wait that runs out: the engine's test hook makes one CTA of the
-  next forward's first fused step expect 16 bytes more than its copies
-  deliver; with a 1 ms wait limit the kernel gives up, drains its copies and
-  returns, the rest of the call's launches return at once, and the forward
-  returns FWI_ERR_CUDA.  The same engine then gives the results of a fresh
-  engine, bit for bit.
+  next forward's first TMA-staged step (the fused step, or the two-pass
+  step's stress pass, whose warps release their stages without a CTA
+  barrier) expect 16 bytes more than its copies deliver; with a 1 ms wait
+  limit the kernel gives up, drains its copies and returns, the rest of the
+  call's launches return at once, and the forward returns FWI_ERR_CUDA.  The
+  same engine then gives the results of a fresh engine, bit for bit.
 * Non-finite values: a NaN placed on the host in a source signal (the forward
   wavefield) or in the observed data (the residual) comes back as
   FWI_ERR_DIVERGED from the device watchdog / the residual check, and the
@@ -38,12 +39,13 @@ def _clean(p, obs, bx=0):
     return rec, mis, g
 
 
-def test_wait_that_runs_out_returns_error_and_engine_recovers():
+@pytest.mark.parametrize("bx", [512, 256])  # fused step, two-pass step
+def test_wait_that_runs_out_returns_error_and_engine_recovers(bx):
     p, obs = _case()
-    want = _clean(p, obs, bx=512)
+    want = _clean(p, obs, bx=bx)
     with Engine(p) as eng:
         eng.set_strategy("binomial", snapshots=6)
-        eng.set_exec(False, 512, 0)  # direct launches of the fused step (the hook's kernel)
+        eng.set_exec(False, bx, 0)  # direct launches
         eng.set_wait_limit(1e-3)
         eng.debug_stall_next()
         with pytest.raises(_capi.FwiError) as ei:
