@@ -858,6 +858,9 @@ struct MultiEngine {
     // ---- forward modelling only -------------------------------------------------
     int forward(double* const* rec_out) {
         FWI_TRY(bind());
+        // the mappings of gradient(), so a forward and a gradient of one engine
+        // compute the same traces bit for bit
+        if (tune_on && !tuned) FWI_TRY(autotune());
         launches_now = 0;
         FWI_TRY(run_phase("fwdonly", [&]() -> int {
             CUDA_TRY(cudaMemsetAsync(d_fwd.p, 0, total_state * 4, stream));

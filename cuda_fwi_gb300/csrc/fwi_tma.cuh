@@ -715,101 +715,29 @@ __device__ __forceinline__ void load_weights(const ItemDesc* items, float2 (&hx)
 // ---------------------------------------------------------------------------
 // Body shared by the passes.  COORDS(t, &b, &x0, &z0) names tile t of the
 // launch (b: its slot or model); ISSUE(b, x0, z0, stage_ptr, bar) queues its
-// copies; COMPUTE(tile, next, stage_ptr) runs its cells (tile and next are
-// (b, x0, z0) of this tile and of the CTA's next one, b = -1 when there is
-// none).  The issuing thread writes each tile's coordinates beside the
-// barriers, so the other threads do no integer division per tile.
-template <int STAGES>
-__host__ __device__ constexpr size_t tma_tail_bytes() {
-    return STAGES * (sizeof(int4) + sizeof(uint64_t));
-}
-
-template <int FP, int STAGE_FLOATS, class Coords, class Issue, class Compute>
-__device__ __forceinline__ void tma_pipeline(int ntiles, int* err, Coords coords, Issue issue, Compute compute,
-                                             unsigned long long wait_ns = 0) {
-    constexpr int kTmaStages = stages_for<STAGE_FLOATS>();
-    const unsigned long long lim = wait_ns ? wait_ns : kWaitNs;
-    static_assert(STAGE_FLOATS % 32 == 0, "stages are 128-byte multiples");
-    // dynamic shared memory only: the stages, the tile coordinates, the barriers
-    extern __shared__ __align__(128) float tma_smem[];
-    int4* crd = reinterpret_cast<int4*>(tma_smem + kTmaStages * STAGE_FLOATS);
-    uint64_t* bar = reinterpret_cast<uint64_t*>(crd + kTmaStages);
-    const int tid = threadIdx.x;
-    // an earlier launch gave up (error word set): return at once, so a failing
-    // pipeline costs one bounded wait and not one per launch; the decision is
-    // CTA-uniform (every thread reaches the barrier below)
-    if (__syncthreads_or(*(volatile int*)err != 0)) return;
-    if (smem_u32(tma_smem) & 127u) {  // TMA destinations need 128-byte alignment
-        if (tid == 0) atomicOr(err, 8);
-        return;
-    }
-    const int first = blockIdx.x, step = gridDim.x;
-    auto issue_tile = [&](int t, int s) {
-        int b, x0, z0;
-        coords(t, &b, &x0, &z0);
-        crd[s] = make_int4(b, x0, z0, 0);
-        issue(b, x0, z0, tma_smem + s * STAGE_FLOATS, &bar[s]);
-    };
-    if (tid == 0) {
-        for (int s = 0; s < kTmaStages; s++) mbar_init(&bar[s], 1);
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        for (int s = 0; s < kTmaStages; s++) {
-            const int t = first + s * step;
-            if (t < ntiles) issue_tile(t, s);
-        }
-    }
-    __syncthreads();
-    for (int k = 0;; k++) {
-        const int t = first + k * step;
-        if (t >= ntiles) break;
-        const int s = k % kTmaStages;
-        const unsigned parity = (unsigned)((k / kTmaStages) & 1);
-        const bool ok = mbar_wait_bounded(&bar[s], parity, lim);
-        if (ok) {
-            // coordinates of this thread's next tile (issued already: stages >= 2)
-            const int4 nx = first + (k + 1) * step < ntiles ? crd[(k + 1) % kTmaStages] : make_int4(-1, 0, 0, 0);
-            compute(crd[s], nx, tma_smem + s * STAGE_FLOATS);
-        }
-        // every thread is done with stage s (or some thread's wait gave up)
-        if (__syncthreads_or(!ok)) {
-            if (tid == 0) {
-                atomicOr(err, 4);
-                // drain the copies this CTA issued and has not consumed (bounded)
-                for (int j = k; j < k + kTmaStages; j++) {
-                    const int tj = first + j * step;
-                    if (tj < ntiles) mbar_wait_bounded(&bar[j % kTmaStages], (unsigned)((j / kTmaStages) & 1), lim);
-                }
-            }
-            return;
-        }
-        if (tid == 0) {
-            const int tn = first + (k + kTmaStages) * step;
-            if (tn < ntiles) {
-                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                issue_tile(tn, s);
-            }
-        }
-    }
-}
-
-// Warp-released variant of the pipeline, for the forward passes (whose tiles
-// read nothing another tile of the launch writes, and whose warps need no
-// data of one another): there is no CTA barrier per tile.  Each warp, once
-// done with a stage, counts itself on the stage's release counter, and the
-// warp that completes the count refills the stage with the CTA's tile S ahead.
-// A warp may so run up to S-1 tiles ahead of the slowest one, instead of every
-// warp of a tile waiting at a barrier for the warps holding its CPML strips.
-// COMPUTE(tile, stage_ptr, k) gets the CTA's tile count k as well, from which
-// the passes rotate the warps' roles: warp w does the rows and columns of
-// warp (w + k) mod nwarps of the plain mapping, so the strip work of edge
-// tiles falls on every warp in turn rather than on the same ones.
+// copies; COMPUTE(tile, next, stage_ptr, k) runs its cells.  The issuing
+// thread writes each tile's coordinates beside the barriers, so the other
+// threads do no integer division per tile.
+// Every pass here reads nothing another tile of its launch writes, and no
+// warp needs data of another, so there is no CTA barrier per tile: each warp,
+// once done with a stage, counts itself on the stage's release counter, and
+// the warp that completes the count refills the stage with the CTA's tile S
+// ahead.  A warp may so run up to S-1 tiles ahead of the slowest one, instead
+// of every warp of a tile waiting at a barrier for the warps holding its CPML
+// strips.  k is the CTA's tile count, from which the passes rotate the warps'
+// roles: warp w does the rows and columns of warp (w + k) mod nwarps of the
+// plain mapping, so the strip work of edge tiles falls on every warp in turn
+// rather than on the same ones.  With NEXT the issuing thread also stores the
+// coordinates of the CTA's following tile beside each stage's own (a warp
+// cannot read them from that tile's stage, which may not be refilled yet);
+// without, next is (-1, 0, 0).
 // A wait that gives up sets bit 2 of the error word and the abort word; the
 // other warps leave at their next tile (or when their own wait gives up, the
 // released count of a stage never completing), and after a CTA barrier one
 // thread waits, bounded, for the last copy issued into each stage.
 template <int STAGES>
-__host__ __device__ constexpr size_t tma_tail_bytes_warps() {
-    return STAGES * (sizeof(int4) + sizeof(uint64_t) + 2 * sizeof(unsigned)) + 16;
+__host__ __device__ constexpr size_t tma_tail_bytes() {
+    return STAGES * (2 * sizeof(int4) + sizeof(uint64_t) + 2 * sizeof(unsigned)) + 16;
 }
 
 __device__ __forceinline__ unsigned atom_add_acq_rel_cta(unsigned* p, unsigned v) {
@@ -821,8 +749,8 @@ __device__ __forceinline__ unsigned atom_add_acq_rel_cta(unsigned* p, unsigned v
     return old;
 }
 
-template <int FP, int STAGE_FLOATS, class Coords, class Issue, class Compute>
-__device__ __forceinline__ void tma_pipeline_warps(int ntiles, int* err, Coords coords, Issue issue,
+template <int FP, int STAGE_FLOATS, bool NEXT = false, class Coords, class Issue, class Compute>
+__device__ __forceinline__ void tma_pipeline(int ntiles, int* err, Coords coords, Issue issue,
                                                    Compute compute, unsigned long long wait_ns = 0,
                                                    int stall = 0) {
     constexpr int S = stages_for<STAGE_FLOATS>();
@@ -830,7 +758,8 @@ __device__ __forceinline__ void tma_pipeline_warps(int ntiles, int* err, Coords 
     static_assert(STAGE_FLOATS % 32 == 0, "stages are 128-byte multiples");
     extern __shared__ __align__(128) float tma_smem[];
     int4* crd = reinterpret_cast<int4*>(tma_smem + S * STAGE_FLOATS);
-    uint64_t* bar = reinterpret_cast<uint64_t*>(crd + S);
+    int4* nxt = crd + S;  // with NEXT: the CTA's tile after the stage's
+    uint64_t* bar = reinterpret_cast<uint64_t*>(nxt + S);
     unsigned* released = reinterpret_cast<unsigned*>(bar + S);  // running count of warps done per stage
     unsigned* issued = released + S;                            // copies issued into each stage
     volatile int* abort = reinterpret_cast<volatile int*>(issued + S);
@@ -846,6 +775,15 @@ __device__ __forceinline__ void tma_pipeline_warps(int ntiles, int* err, Coords 
         int b, x0, z0;
         coords(t, &b, &x0, &z0);
         crd[s] = make_int4(b, x0, z0, 0);
+        if constexpr (NEXT) {
+            if (t + step < ntiles) {
+                int b1, x1, z1;
+                coords(t + step, &b1, &x1, &z1);
+                nxt[s] = make_int4(b1, x1, z1, 0);
+            } else {
+                nxt[s] = make_int4(-1, 0, 0, 0);
+            }
+        }
         issued[s] += 1u;
         issue(b, x0, z0, tma_smem + s * STAGE_FLOATS, &bar[s]);
     };
@@ -875,7 +813,7 @@ __device__ __forceinline__ void tma_pipeline_warps(int ntiles, int* err, Coords 
             }
             break;
         }
-        compute(crd[s], tma_smem + s * STAGE_FLOATS, k);
+        compute(crd[s], NEXT ? nxt[s] : make_int4(-1, 0, 0, 0), tma_smem + s * STAGE_FLOATS, k);
         // the warp's reads of stage s are done; the release (acq_rel atomic)
         // orders them before the refill's async-proxy writes
         __syncwarp();
@@ -894,22 +832,23 @@ __device__ __forceinline__ void tma_pipeline_warps(int ntiles, int* err, Coords 
     }
 }
 
-// Logical thread of the plain forward mapping that thread threadIdx.x plays
-// in the CTA's k-th tile (warp rotation, above).
+// Logical thread of the plain mapping (NT threads) that thread threadIdx.x
+// plays in the CTA's k-th tile (warp rotation, above).
+template <int NT = kFwdThreads>
 __device__ __forceinline__ int rotated_thread(int k) {
-    static_assert((kFwdThreads & (kFwdThreads - 1)) == 0, "the rotation wraps a power of two");
-    return (int)((threadIdx.x + ((unsigned)k << 5)) & (kFwdThreads - 1));
+    static_assert((NT & (NT - 1)) == 0, "the rotation wraps a power of two");
+    return (int)((threadIdx.x + ((unsigned)k << 5)) & (NT - 1));
 }
 
 template <int FP>
 constexpr size_t stress_tma_smem() {
     constexpr int S = stages_for<TmaGeom<FP>::S_STAGE>();
-    return sizeof(float) * S * TmaGeom<FP>::S_STAGE + tma_tail_bytes_warps<S>();
+    return sizeof(float) * S * TmaGeom<FP>::S_STAGE + tma_tail_bytes<S>();
 }
 template <int FP>
 constexpr size_t velocity_tma_smem() {
     constexpr int S = stages_for<TmaGeom<FP>::V_STAGE>();
-    return sizeof(float) * S * TmaGeom<FP>::V_STAGE + tma_tail_bytes_warps<S>();
+    return sizeof(float) * S * TmaGeom<FP>::V_STAGE + tma_tail_bytes<S>();
 }
 static_assert(stress_tma_smem<4>() <= 232448 && velocity_tma_smem<4>() <= 232448, "shared memory per CTA");
 static_assert(stress_tma_smem<6>() <= 232448 && velocity_tma_smem<6>() <= 232448, "shared memory per CTA");
@@ -921,12 +860,12 @@ __global__ void __launch_bounds__(kFwdThreads, 1)
     using G = TmaGeom<FP>;
     float2 hx[FP], hz[FP];
     load_weights<FP>(items, hx, hz);
-    tma_pipeline_warps<FP, G::S_STAGE>(
+    tma_pipeline<FP, G::S_STAGE>(
         g.ntiles, err, [&](int t, int* b, int* x0, int* z0) { tile_coords(g, t, b, x0, z0, FP, kTmaTZ); },
         [&](int b, int x0, int z0, float* st, uint64_t* bar) {
             stress_issue<FP>(maps, items + b, b, x0, z0, st, bar);
         },
-        [&](int4 c, const float* st, int k) {
+        [&](int4 c, int4, const float* st, int k) {
             stress_compute<FP>(*reinterpret_cast<const ItemDesc*>(st + G::S_DESC), g, st, c.y, c.z, it, flags, hx,
                                hz, rotated_thread(k));
         },
@@ -941,12 +880,12 @@ __global__ void __launch_bounds__(kFwdThreads, 1)
     const bool we = (flags & FL_WE) != 0;
     float2 hx[FP], hz[FP];
     load_weights<FP>(items, hx, hz);
-    tma_pipeline_warps<FP, G::V_STAGE>(
+    tma_pipeline<FP, G::V_STAGE>(
         g.ntiles, err, [&](int t, int* b, int* x0, int* z0) { tile_coords(g, t, b, x0, z0, FP, kTmaTZ); },
         [&](int b, int x0, int z0, float* st, uint64_t* bar) {
             velocity_issue<FP>(maps, items + b, b, x0, z0, st, bar, we);
         },
-        [&](int4 c, const float* st, int k) {
+        [&](int4 c, int4, const float* st, int k) {
             velocity_compute<FP>(*reinterpret_cast<const ItemDesc*>(st + G::V_DESC), g, st, c.y, c.z, flags, hx, hz,
                                  rotated_thread(k));
         },
@@ -1020,8 +959,8 @@ static_assert((kTmaTX / 2) * kAdjTZ == kAdjThreads, "one thread per column pair 
 
 // The warp's cells are plain-stencil cells and, on a gradient step, lie in
 // the gradient window sampled at unit intervals.
-__device__ __forceinline__ bool interior_warp_adj(const TmaGrid& g, int x0, int z0, bool grad_step) {
-    const int w = threadIdx.x >> 5;
+__device__ __forceinline__ bool interior_warp_adj(const TmaGrid& g, int x0, int z0, bool grad_step, int lt) {
+    const int w = lt >> 5;
     const int wx0 = x0 + (w & 1) * 64, wz = z0 + (w >> 1);
     bool in = wx0 >= g.cxl && wx0 + 63 <= g.cxh && wz >= g.czl && wz <= g.czh;
     if (grad_step) in = in && wx0 >= g.gxl && wx0 + 63 <= g.gxh && wz >= g.gzl && wz <= g.gzh;
@@ -1050,11 +989,12 @@ __device__ __forceinline__ float rcp_approx(float x) {
 
 template <int FP, bool INTERIOR, bool GRAD>
 __device__ __forceinline__ void adjoint_rows(const ItemDesc& D, const float* st, int x0, int z0,
-                                             const float2 (&hx)[FP], const float2 (&hz)[FP], const GradAhead& ga) {
+                                             const float2 (&hx)[FP], const float2 (&hz)[FP], const GradAhead& ga,
+                                             int lt) {
     constexpr bool grad_step = GRAD;
     using G = AdjGeom<FP>;
-    const int cp = (threadIdx.x & (kTmaTX / 2 - 1)) * 2;
-    const int r = threadIdx.x / (kTmaTX / 2);  // tile row
+    const int cp = (lt & (kTmaTX / 2 - 1)) * 2;
+    const int r = lt / (kTmaTX / 2);  // tile row
     const int ix = x0 + cp, iz = z0 + r;
     const int P = D.pitch, tp = D.tp;
     PairCols pc = {true, true, {-1, -1}};
@@ -1235,26 +1175,29 @@ __global__ void __launch_bounds__(kAdjThreads, 1)
     const int wx1 = __ldg(&items[0].wx1), wz1 = __ldg(&items[0].wz1), nfx = __ldg(&items[0].nfx);
     GradAhead ga;
     ga.valid = false;
-    tma_pipeline<FP, G::STAGE>(
+    tma_pipeline<FP, G::STAGE, true>(
         g.ntiles, err, [&](int t, int* b, int* x0, int* z0) { tile_coords(g, t, b, x0, z0, FP, kAdjTZ); },
         [&](int b, int x0, int z0, float* st, uint64_t* bar) {
             adjoint_issue<FP>(maps, items + b, b, x0, z0, st, bar, grad);
         },
-        [&](int4 c, int4 n, const float* st) {
+        [&](int4 c, int4 n, const float* st, int k) {
             const ItemDesc& D = *reinterpret_cast<const ItemDesc*>(st + G::DESC);
-            const bool in = interior_warp_adj(g, c.y, c.z, grad);
+            const int lt = rotated_thread<kAdjThreads>(k);
+            const bool in = interior_warp_adj(g, c.y, c.z, grad, lt);
             if (grad) {
-                if (in) adjoint_rows<FP, true, true>(D, st, c.y, c.z, hx, hz, ga);
-                else adjoint_rows<FP, false, true>(D, st, c.y, c.z, hx, hz, ga);
+                if (in) adjoint_rows<FP, true, true>(D, st, c.y, c.z, hx, hz, ga, lt);
+                else adjoint_rows<FP, false, true>(D, st, c.y, c.z, hx, hz, ga, lt);
             } else {
-                if (in) adjoint_rows<FP, true, false>(D, st, c.y, c.z, hx, hz, ga);
-                else adjoint_rows<FP, false, false>(D, st, c.y, c.z, hx, hz, ga);
+                if (in) adjoint_rows<FP, true, false>(D, st, c.y, c.z, hx, hz, ga, lt);
+                else adjoint_rows<FP, false, false>(D, st, c.y, c.z, hx, hz, ga, lt);
             }
             ga.valid = false;
-            if (grad && n.x >= 0 && interior_warp_adj(g, n.y, n.z, true)) {
+            // gradient samples of this thread's cells in the CTA's next tile
+            // (its role there is that of rotation k + 1)
+            const int ln = rotated_thread<kAdjThreads>(k + 1);
+            if (grad && n.x >= 0 && interior_warp_adj(g, n.y, n.z, true, ln)) {
                 const ItemDesc* In = items + n.x;
-                const int gi = (n.z + (int)(threadIdx.x / (kTmaTX / 2)) - wz1) * nfx +
-                               (n.y + (int)(threadIdx.x & (kTmaTX / 2 - 1)) * 2 - wx1);
+                const int gi = (n.z + ln / (kTmaTX / 2) - wz1) * nfx + (n.y + (ln & (kTmaTX / 2 - 1)) * 2 - wx1);
                 const float* gl = ldg_ptr(&In->glam);
                 const float* gm = ldg_ptr(&In->gmu);
                 const float* gr = ldg_ptr(&In->grho);
@@ -1332,7 +1275,7 @@ __global__ void __launch_bounds__(kFwdThreads, 1)
                             unsigned flags, long long msrc, int* err) {
     const MultiMaps* maps = mx;
     using G = TmaGeom<FP>;
-    tma_pipeline_warps<FP, G::S_STAGE>(
+    tma_pipeline<FP, G::S_STAGE>(
         ntiles, err,
         [&](int t, int* b, int* x0, int* z0) {
             const Tile T = tiles[t];
@@ -1343,7 +1286,7 @@ __global__ void __launch_bounds__(kFwdThreads, 1)
         [&](int b, int x0, int z0, float* st, uint64_t* bar) {
             stress_issue<FP>(maps[b].sf, items + b, 0, x0, z0, st, bar);
         },
-        [&](int4 c, const float* st, int k) {
+        [&](int4 c, int4, const float* st, int k) {
             const ItemDesc& D = *reinterpret_cast<const ItemDesc*>(st + G::S_DESC);
             float2 hx[FP], hz[FP];
             staged_weights<FP>(D, hx, hz);
@@ -1360,7 +1303,7 @@ __global__ void __launch_bounds__(kFwdThreads, 1)
                               unsigned flags, int adj, long long msrc, int* err) {
     using G = TmaGeom<FP>;
     const bool we = (flags & FL_WE) != 0;
-    tma_pipeline_warps<FP, G::V_STAGE>(
+    tma_pipeline<FP, G::V_STAGE>(
         ntiles, err,
         [&](int t, int* b, int* x0, int* z0) {
             const Tile T = tiles[t];
@@ -1372,7 +1315,7 @@ __global__ void __launch_bounds__(kFwdThreads, 1)
             if (adj) velocity_issue<FP>(mx[b].va, items + b, 0, x0, z0, st, bar, we);
             else velocity_issue2<FP>(my[b].vf, mx[b].vf, items + b, 0, x0, z0, st, bar, we);
         },
-        [&](int4 c, const float* st, int k) {
+        [&](int4 c, int4, const float* st, int k) {
             const ItemDesc& D = *reinterpret_cast<const ItemDesc*>(st + G::V_DESC);
             float2 hx[FP], hz[FP];
             staged_weights<FP>(D, hx, hz);
@@ -1404,17 +1347,18 @@ __global__ void __launch_bounds__(kAdjThreads, 1)
         [&](int b, int x0, int z0, float* st, uint64_t* bar) {
             adjoint_issue<FP>(maps[b].a, items + b, 0, x0, z0, st, bar, grad);
         },
-        [&](int4 c, int4, const float* st) {
+        [&](int4 c, int4, const float* st, int k) {
             const ItemDesc& D = *reinterpret_cast<const ItemDesc*>(st + G::DESC);
             float2 hx[FP], hz[FP];
             staged_weights<FP>(D, hx, hz);
-            const bool in = interior_warp_adj(model_ranges(D), c.y, c.z, grad);
+            const int lt = rotated_thread<kAdjThreads>(k);
+            const bool in = interior_warp_adj(model_ranges(D), c.y, c.z, grad, lt);
             if (grad) {
-                if (in) adjoint_rows<FP, true, true>(D, st, c.y, c.z, hx, hz, none);
-                else adjoint_rows<FP, false, true>(D, st, c.y, c.z, hx, hz, none);
+                if (in) adjoint_rows<FP, true, true>(D, st, c.y, c.z, hx, hz, none, lt);
+                else adjoint_rows<FP, false, true>(D, st, c.y, c.z, hx, hz, none, lt);
             } else {
-                if (in) adjoint_rows<FP, true, false>(D, st, c.y, c.z, hx, hz, none);
-                else adjoint_rows<FP, false, false>(D, st, c.y, c.z, hx, hz, none);
+                if (in) adjoint_rows<FP, true, false>(D, st, c.y, c.z, hx, hz, none, lt);
+                else adjoint_rows<FP, false, false>(D, st, c.y, c.z, hx, hz, none, lt);
             }
         });
 }

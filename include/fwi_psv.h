@@ -358,9 +358,10 @@ int fwi_psv_step_search(double est, double L2_0, fwi_psv_trial_fn trial, void* c
  * per-shot call (forward_kernel_PSV_GPU + adjoint_kernel_PSV_GPU with the
  * reference gradient, fwi intervals 1, window = the padded grid from the free
  * surface down).  The thread mapping and tile height of each fdorder group are
- * chosen by timing the candidates on the group's own tiles (autotune != 0),
- * cached in a JSON file ($FWI_PSV_TUNE_CACHE, default
- * ~/.cache/cuda_fwi_gb300/autotune.json) keyed by GPU and group shape. */
+ * chosen by timing the candidates on the group's own tiles (autotune != 0;
+ * at the engine's first forward or gradient, so both run the same mappings and
+ * compute the same traces), cached in a JSON file ($FWI_PSV_TUNE_CACHE,
+ * default ~/.cache/cuda_fwi_gb300/autotune.json) keyed by GPU and group shape. */
 typedef struct fwi_psv_model {
     fwi_psv_desc grid;                 /* as for fwi_psv_create */
     const double *lam, *mu, *rho;      /* [nzt][nxt] */
