@@ -16,10 +16,12 @@ import numpy as np
 _PKG = Path(__file__).resolve().parent
 LIB_PATH = _PKG / "_lib" / "libfwi_psv.so"
 
+ABI_VERSION = 2  # FWI_PSV_ABI_VERSION of include/fwi_psv.h this binding follows
 FWI_OK = 0
 ERRORS = {
     -1: "FWI_ERR_INVALID", -2: "FWI_ERR_UNSUPPORTED", -3: "FWI_ERR_NOMEM", -4: "FWI_ERR_CUDA",
     -5: "FWI_ERR_STATE", -6: "FWI_ERR_DIVERGED", -7: "FWI_ERR_NOFORWARD", -8: "FWI_ERR_NODEVICE",
+    -9: "FWI_ERR_IO",
 }
 FWI_STORE_FULL, FWI_STORE_BINOMIAL, FWI_STORE_RANDOM = 0, 1, 2
 FWI_GRAD_REFERENCE, FWI_GRAD_EXACT = 0, 1
@@ -63,7 +65,8 @@ class Layout(C.Structure):
 class FwiOpts(C.Structure):
     _fields_ = [("max_iter", C.c_int), ("max_error", C.c_double), ("step_length", C.c_double),
                 ("order", C.c_int), ("trial_misfit", C.c_int), ("precondition", C.c_int),
-                ("true_lam", dp), ("true_mu", dp), ("true_rho", dp), ("restart_step", C.c_double)]
+                ("true_lam", dp), ("true_mu", dp), ("true_rho", dp), ("restart_step", C.c_double),
+                ("resume_file", C.c_char_p)]
 
 
 class FwiIter(C.Structure):
@@ -72,6 +75,8 @@ class FwiIter(C.Structure):
 
 
 TRIAL_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_double, dp)
+ALLOC_FN = C.CFUNCTYPE(C.c_void_p, C.c_size_t, C.c_void_p)
+FREE_FN = C.CFUNCTYPE(None, C.c_void_p, C.c_void_p)
 
 
 class Model(C.Structure):
@@ -110,6 +115,7 @@ _SIGS = {
     "fwi_psv_get_stats": (C.c_int, [C.c_void_p, C.POINTER(Stats)]),
     "fwi_psv_time_kernels": (C.c_int, [C.c_void_p, C.c_int, dp]),
     "fwi_psv_set_wait_limit": (C.c_int, [C.c_void_p, C.c_double]),
+    "fwi_psv_set_device_allocator": (C.c_int, [ALLOC_FN, FREE_FN, C.c_void_p]),
     "fwi_psv_debug_stall_next": (C.c_int, [C.c_void_p]),
     "fwi_psv_misfit_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_double,
                                          C.c_void_p, dp, C.c_void_p]),
@@ -155,6 +161,9 @@ def lib():
             fn = getattr(L, name)
             fn.restype = res
             fn.argtypes = args
+        if L.fwi_psv_abi_version() != ABI_VERSION:
+            raise FwiLibraryMissing(f"{path} has ABI version {L.fwi_psv_abi_version()}, this binding "
+                                    f"{ABI_VERSION}: rebuild it")
         _lib = L
     return _lib
 

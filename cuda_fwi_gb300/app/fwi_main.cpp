@@ -373,7 +373,7 @@ int main(int argc, char** argv) {
         if ((rc = check(fwi_psv_set_fwi(e, c.fdt, c.fdx, c.fdz, c.x1, c.x2, c.z1, c.z2), "set_fwi"))) break;
         if ((rc = check(fwi_psv_set_strategy(e, FWI_STORE_BINOMIAL, c.checkpoints, 0), "set_strategy"))) break;
         mkdirs(out + "/io/density_snap");
-        fwi_psv_fwi_opts o = {1, c.max_error, 0.01, c.order, c.trial, 1, nullptr, nullptr, nullptr, 0.0};
+        fwi_psv_fwi_opts o = {1, c.max_error, 0.01, c.order, c.trial, 1, nullptr, nullptr, nullptr, 0.0, nullptr};
         std::vector<fwi_psv_fwi_iter> log((size_t)c.nshots);
         bool converged = false;
         for (int iter = 1; iter <= c.max_iter && !rc; iter++) {

@@ -27,7 +27,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O2,-ffp-contract=off",
            "--expt-relaxed-constexpr", f"-I{ROOT / 'include'}", f"-I{CSRC}"]
 UNITS = ["fwi_engine.cu", "fwi_host.cpp", "fwi_refshim.cpp", "fwi_noalloc.cu", "fwi_optim.cu"]
-HEADERS = ["fwi_kernels.cuh", "fwi_exact.cuh", "fwi_tma.cuh", "fwi_multi.cuh", "fwi_host.h"]
+HEADERS = ["fwi_kernels.cuh", "fwi_exact.cuh", "fwi_tma.cuh", "fwi_fused.cuh", "fwi_multi.cuh", "fwi_host.h",
+           "fwi_alloc.hpp"]
 APP_DIR = PKG / "app"
 APP = OUT_DIR / "fwi_run"
 REF_DRIVER = OUT_DIR / "ref_driver"

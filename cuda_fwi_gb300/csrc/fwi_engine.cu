@@ -24,6 +24,7 @@
 #include <vector>
 
 #include "../../include/fwi_psv.h"
+#include "fwi_alloc.hpp"
 #include "fwi_host.h"
 #include "fwi_exact.cuh"
 #include "fwi_kernels.cuh"
@@ -602,12 +603,13 @@ static ExactSet exact_for(int fp) {
 struct DBuf {
     void* p = nullptr;
     size_t bytes = 0;
+    DeviceAllocator al;  // the allocator that made p
     DBuf() = default;
     DBuf(const DBuf&) = delete;
     DBuf& operator=(const DBuf&) = delete;
     ~DBuf() { release(); }
     void release() {
-        if (p) cudaFree(p);
+        device_free(p, al);
         p = nullptr;
         bytes = 0;
     }
@@ -615,12 +617,14 @@ struct DBuf {
         if (n <= bytes && p) return FWI_OK;
         release();
         if (n == 0) return FWI_OK;
-        cudaError_t e = cudaMalloc(&p, n);
+        cudaError_t e = device_alloc(&p, n, &al);
         if (e != cudaSuccess) {
             p = nullptr;
             cudaGetLastError();
-            return fail(FWI_ERR_NOMEM, "cudaMalloc of " + std::to_string(n) + " bytes failed: " +
-                                           cudaGetErrorString(e));
+            return fail(FWI_ERR_NOMEM, "device allocation of " + std::to_string(n) + " bytes failed: " +
+                                           (e == cudaErrorMisalignedAddress
+                                                ? std::string("the allocator's pointer is not 256-byte aligned")
+                                                : std::string(cudaGetErrorString(e))));
         }
         bytes = n;
         return FWI_OK;
@@ -2390,6 +2394,7 @@ const char* fwi_psv_strerror(int s) {
         case FWI_ERR_DIVERGED: return "wavefield diverged";
         case FWI_ERR_NOFORWARD: return "no retained forward pass";
         case FWI_ERR_NODEVICE: return "no CUDA device";
+        case FWI_ERR_IO: return "file not written";
     }
     return "unknown status";
 }
@@ -2719,6 +2724,17 @@ int fwi_psv_set_exec(fwi_psv_engine* h, int use_graphs, int block_x, int tile_z,
     e.invalidate_batch();
     for (auto& kv : e.tilesets) kv.second->ntiles = 0;
     e.drop_graphs();
+    return FWI_OK;
+}
+
+int fwi_psv_set_device_allocator(fwi_psv_alloc_fn alloc, fwi_psv_free_fn release, void* ctx) {
+    if ((alloc == nullptr) != (release == nullptr))
+        return fail(FWI_ERR_INVALID, "give both alloc and release, or neither");
+    fwi::DeviceAllocator a;
+    a.alloc = alloc;
+    a.release = release;
+    a.ctx = alloc ? ctx : nullptr;
+    fwi::set_device_allocator(a);
     return FWI_OK;
 }
 

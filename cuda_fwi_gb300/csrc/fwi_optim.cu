@@ -19,11 +19,13 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <string>
 #include <vector>
 
 #include "../../include/fwi_psv.h"
+#include "fwi_alloc.hpp"
 #include "fwi_host.h"
 
 namespace {
@@ -95,14 +97,16 @@ __global__ void partial_sums_kernel(const double* __restrict__ a, size_t n, doub
 
 struct DevBuf {
     void* p = nullptr;
-    ~DevBuf() {
-        if (p) cudaFree(p);
-    }
+    fwi::DeviceAllocator al;  // the allocator that made p
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    ~DevBuf() { fwi::device_free(p, al); }
     int alloc(size_t bytes) {
-        if (cudaMalloc(&p, bytes) != cudaSuccess) {
+        if (fwi::device_alloc(&p, bytes, &al) != cudaSuccess) {
             p = nullptr;
             cudaGetLastError();
-            return fwi::fail(FWI_ERR_NOMEM, "cudaMalloc of " + std::to_string(bytes) + " bytes failed");
+            return fwi::fail(FWI_ERR_NOMEM, "device allocation of " + std::to_string(bytes) + " bytes failed");
         }
         return FWI_OK;
     }
@@ -337,6 +341,66 @@ extern "C" int fwi_psv_step_search(double est, double L2_0, fwi_psv_trial_fn tri
     return FWI_OK;
 }
 
+// ---------------------------------------------------------------------------
+// FWI-iteration resume file (no reference counterpart)
+// ---------------------------------------------------------------------------
+// Layout: a header, `entries` log records, then lam, mu, rho ([nzt][nxt] FP64).
+// The header carries what the continuation must match (cells, shots, order,
+// trial mode, preconditioning, the first step estimate) and the loop state.
+struct ResumeHeader {
+    char magic[8];
+    long long cells;
+    int nshots, order, trial, precondition;
+    int iters_done, entries, stopped, pad;
+    double step_length0, step;
+};
+static const char kResumeMagic[8] = {'F', 'W', 'I', 'P', 'S', 'V', 'R', '1'};
+
+static bool resume_matches(const ResumeHeader& h, const fwi_psv_fwi_opts* o, size_t cells, int nshots) {
+    return std::memcmp(h.magic, kResumeMagic, 8) == 0 && h.cells == (long long)cells && h.nshots == nshots &&
+           h.order == o->order && h.trial == o->trial_misfit && h.precondition == o->precondition &&
+           h.step_length0 == o->step_length && h.iters_done >= 0 && h.entries >= 0;
+}
+
+// Write the state (the model from the device) beside the file, then rename it
+// over the file, so an interrupted write leaves the previous state.
+static int resume_save(const char* path, const ResumeHeader& h, const fwi_psv_fwi_iter* log,
+                       const std::vector<double>* model) {
+    const std::string tmp = std::string(path) + ".tmp";
+    FILE* f = std::fopen(tmp.c_str(), "wb");
+    if (!f) return fwi::fail(FWI_ERR_IO, "cannot write the resume file " + tmp);
+    bool ok = std::fwrite(&h, sizeof(h), 1, f) == 1;
+    if (h.entries > 0) ok = ok && std::fwrite(log, sizeof(fwi_psv_fwi_iter), h.entries, f) == (size_t)h.entries;
+    for (int q = 0; q < 3; q++) ok = ok && std::fwrite(model[q].data(), 8, model[q].size(), f) == model[q].size();
+    ok = (std::fclose(f) == 0) && ok;
+    if (!ok || std::rename(tmp.c_str(), path) != 0) {
+        std::remove(tmp.c_str());
+        return fwi::fail(FWI_ERR_IO, std::string("cannot write the resume file ") + path);
+    }
+    return FWI_OK;
+}
+
+// Read a resume file if there is one: *found = false when the file does not
+// exist; FWI_ERR_INVALID when it belongs to another run or is cut short.
+static int resume_load(const char* path, const fwi_psv_fwi_opts* o, size_t cells, int nshots, int capacity,
+                       ResumeHeader* h, fwi_psv_fwi_iter* log, std::vector<double>* model, bool* found) {
+    *found = false;
+    FILE* f = std::fopen(path, "rb");
+    if (!f) return FWI_OK;
+    bool ok = std::fread(h, sizeof(*h), 1, f) == 1 && resume_matches(*h, o, cells, nshots) &&
+              h->entries <= capacity;
+    if (ok && h->entries > 0) ok = std::fread(log, sizeof(fwi_psv_fwi_iter), h->entries, f) == (size_t)h->entries;
+    for (int q = 0; q < 3 && ok; q++) {
+        model[q].resize(cells);
+        ok = std::fread(model[q].data(), 8, cells, f) == cells;
+    }
+    std::fclose(f);
+    if (!ok) return fwi::fail(FWI_ERR_INVALID, std::string("the resume file ") + path +
+                                                   " does not belong to this run (grid, shots or options) or is cut short");
+    *found = true;
+    return FWI_OK;
+}
+
 extern "C" int fwi_psv_fwi_run(fwi_psv_engine* e, const fwi_psv_fwi_opts* o, int nshots, const int* ids,
                                const double* obs, double* lam, double* mu, double* rho, fwi_psv_fwi_iter* log,
                                int* done) {
@@ -352,14 +416,36 @@ extern "C" int fwi_psv_fwi_run(fwi_psv_engine* e, const fwi_psv_fwi_opts* o, int
     d.obs = obs;
     d.trial_mode = o->trial_misfit;
     double* host[3] = {lam, mu, rho};
+    double step = o->step_length;
+    int entries = 0, iter0 = 0;
+    bool stop = false;
+    ResumeHeader rh{};
+    std::vector<double> rm[3];
+    const int capacity = o->max_iter * (o->order == FWI_ORDER_SUMMED ? 1 : nshots);
+    if (o->resume_file) {
+        bool found = false;
+        OPT_TRY(resume_load(o->resume_file, o, d.n, nshots, capacity, &rh, log, rm, &found));
+        if (found) {
+            for (int q = 0; q < 3; q++) std::memcpy(host[q], rm[q].data(), d.n * 8);
+            step = rh.step;
+            entries = rh.entries;
+            iter0 = rh.iters_done;
+            stop = rh.stopped != 0;
+        } else {
+            std::memcpy(rh.magic, kResumeMagic, 8);
+            rh.cells = (long long)d.n;
+            rh.nshots = nshots;
+            rh.order = o->order;
+            rh.trial = o->trial_misfit;
+            rh.precondition = o->precondition;
+            rh.step_length0 = o->step_length;
+        }
+    }
     for (int q = 0; q < 3; q++) {
         OPT_CUDA(cudaMemcpy(d.cur[q].p, host[q], d.n * 8, cudaMemcpyHostToDevice));
         OPT_CUDA(cudaMemcpy(d.old[q].p, host[q], d.n * 8, cudaMemcpyHostToDevice));
     }
-    double step = o->step_length;
-    int entries = 0;
-    bool stop = false;
-    for (int iter = 0; iter < o->max_iter && !stop; iter++) {
+    for (int iter = iter0; iter < o->max_iter && !stop; iter++) {
         double c[3];
         OPT_TRY(d.medium_average(c));
         OPT_TRY(d.materials(d.cur));
@@ -414,6 +500,17 @@ extern "C" int fwi_psv_fwi_run(fwi_psv_engine* e, const fwi_psv_fwi_opts* o, int
             rec.model_error = d.model_error(o);
             rec.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
             entries++;
+        }
+        if (o->resume_file) {
+            rh.iters_done = iter + 1;
+            rh.entries = entries;
+            rh.stopped = stop ? 1 : 0;
+            rh.step = step;
+            for (int q = 0; q < 3; q++) {
+                rm[q].resize(d.n);
+                OPT_CUDA(cudaMemcpy(rm[q].data(), d.cur[q].p, d.n * 8, cudaMemcpyDeviceToHost));
+            }
+            OPT_TRY(resume_save(o->resume_file, rh, log, rm));
         }
     }
     for (int q = 0; q < 3; q++) OPT_CUDA(cudaMemcpy(host[q], d.cur[q].p, d.n * 8, cudaMemcpyDeviceToHost));

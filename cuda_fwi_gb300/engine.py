@@ -182,17 +182,19 @@ class Engine:
                                                    C.c_void_p(rho.data_ptr())), "set_model_device")
 
     def fwi_run(self, shots, obs, max_iter, step_length=0.01, max_error=0.0, order="summed", trial="sum",
-                precondition=True, model=None, true_model=None, restart_step=0.0):
+                precondition=True, model=None, true_model=None, restart_step=0.0, resume_file=None):
         """The inversion loop on the device.  model = (lam, mu, rho) start
         (default: the problem's); returns ((lam, mu, rho), log) with one dict
         per update (misfit, step_length, trials, status, model_error, seconds).
-        restart_step > 0 retries a failed step search once from that step."""
+        restart_step > 0 retries a failed step search once from that step.
+        resume_file: the loop state is saved there after each iteration, and a
+        run that finds it continues from it (to max_iter iterations in all)."""
         ids = _i32(shots)
         lam, mu, rho = [np.array(x, np.float64, order="C") for x in (model or (self.p.lam, self.p.mu, self.p.rho))]
         tm = [_f64(x) for x in true_model] if true_model is not None else [None] * 3
         o = _capi.FwiOpts(max_iter, max_error, step_length, {"summed": 0, "per_shot": 1}[order],
                           {"sum": 0, "last": 1}[trial], int(precondition), pd(tm[0]), pd(tm[1]), pd(tm[2]),
-                          float(restart_step))
+                          float(restart_step), None if resume_file is None else str(resume_file).encode())
         n = max_iter * (len(ids) if order == "per_shot" else 1)
         log = (_capi.FwiIter * max(n, 1))()
         done = C.c_int()

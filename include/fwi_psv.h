@@ -44,7 +44,7 @@
 extern "C" {
 #endif
 
-#define FWI_PSV_ABI_VERSION 1
+#define FWI_PSV_ABI_VERSION 2
 
 enum {
     FWI_OK = 0,
@@ -55,7 +55,8 @@ enum {
     FWI_ERR_STATE = -5,       /* call out of order (e.g. backward before forward) */
     FWI_ERR_DIVERGED = -6,    /* |syn-obs| > 1e10, where the reference exits */
     FWI_ERR_NOFORWARD = -7,   /* backward without a retained forward */
-    FWI_ERR_NODEVICE = -8     /* no CUDA device / driver */
+    FWI_ERR_NODEVICE = -8,    /* no CUDA device / driver */
+    FWI_ERR_IO = -9           /* a file could not be written (the FWI resume file) */
 };
 
 /* ---- setup helpers (host) ---------------------------------------------- */
@@ -83,6 +84,26 @@ int fwi_psv_wavelet(double* signal, int nt, double dt, double amp, double fc, do
 /* fd_medium.cu:128-159 on the host (FP64); outputs [nzt-1][nxt-1]. */
 int fwi_psv_average_parameters(int nzt, int nxt, const double* mu, const double* rho,
                                double* mu_zx, double* rho_zp, double* rho_xp);
+
+/* ---- device memory ------------------------------------------------------ */
+
+/* No counterpart in the reference (which calls cudaMalloc directly and exits
+ * when it fails, forward_kernel_PSV_GPU.cu:19-27).  Once set, every device
+ * allocation of the library's engines, multi-model engines and FWI loop goes
+ * through alloc(bytes, ctx) and is returned through release(ptr, ctx): an
+ * application's pool allocator, for example.  alloc returns device memory of
+ * the current device aligned to 256 bytes, or NULL; a NULL (or a misaligned
+ * pointer, handed back at once) makes the call that needed the memory return
+ * FWI_ERR_NOMEM, and the engine stays usable.  A buffer is released through
+ * the allocator that made it, even after a later change (so release and ctx
+ * must stay valid while an engine made under them lives), and only after the
+ * device has been synchronised (as cudaFree does).  alloc = release = NULL
+ * restores cudaMalloc / cudaFree.  Set it between calls, not while
+ * another thread runs one.  (The caller's d_* buffers of the
+ * reference-signature calls are the caller's, as in the reference.) */
+typedef void* (*fwi_psv_alloc_fn)(size_t bytes, void* ctx);
+typedef void (*fwi_psv_free_fn)(void* ptr, void* ctx);
+int fwi_psv_set_device_allocator(fwi_psv_alloc_fn alloc, fwi_psv_free_fn release, void* ctx);
 
 /* ---- engine ------------------------------------------------------------ */
 
@@ -319,6 +340,15 @@ typedef struct fwi_psv_fwi_opts {
                             * same gradient, from this step-length estimate (e.g. the initial one,
                             * after the searches' starting steps have shrunk); 0 stops there, as
                             * the reference would (status 1) */
+    const char* resume_file; /* no counterpart in the reference (whose per-iteration model CSVs,
+                            * fd_wave_model.cu:919-952, have no loader): when not NULL, after each
+                            * completed iteration the loop state -- iterations done, the next
+                            * search's starting step, whether the loop stopped, the log so far and
+                            * the model -- replaces this file (written beside it and renamed); a
+                            * run that finds the file continues from it (the model arguments'
+                            * values are then replaced by the file's) until max_iter iterations in
+                            * all, giving the log and model of an uninterrupted run.  A file of
+                            * another grid or option set is FWI_ERR_INVALID. */
 } fwi_psv_fwi_opts;
 typedef struct fwi_psv_fwi_iter {
     double misfit;         /* summed shot misfit at the model the gradient was taken at */

@@ -40,7 +40,7 @@ def test_cpp_reference_shims_exported():
 
 def test_abi_version_and_strerror():
     L = _capi.lib()
-    assert L.fwi_psv_abi_version() == 1
+    assert L.fwi_psv_abi_version() == _capi.ABI_VERSION == 2
     assert L.fwi_psv_strerror(0) == b"ok"
     assert L.fwi_psv_strerror(-3) == b"out of memory"
 
@@ -163,3 +163,19 @@ def test_plan_restatement_matches_library(n, s):
         k += 1
     want = (n - 1 - last) + sum(b - a for (kind, a, b) in plan[k:] if kind == 0)
     assert _plan.recompute_after_first_sweep(n, s) == want
+
+
+def test_device_allocator_hook_arguments():
+    """fwi_psv_set_device_allocator: both callbacks or neither (no GPU needed:
+    the hook is only recorded here)."""
+    from cuda_fwi_gb300 import allocator as A
+    L = _capi.lib()
+    keep = (_capi.ALLOC_FN(lambda n, c: None), _capi.FREE_FN(lambda p, c: None))
+    assert L.fwi_psv_set_device_allocator(keep[0], _capi.FREE_FN(), None) == -1
+    assert L.fwi_psv_set_device_allocator(_capi.ALLOC_FN(), keep[1], None) == -1
+    assert L.fwi_psv_set_device_allocator(keep[0], keep[1], None) == 0
+    assert L.fwi_psv_set_device_allocator(_capi.ALLOC_FN(), _capi.FREE_FN(), None) == 0
+    A.set_device_allocator(lambda n: 0, lambda p: None)
+    A.set_device_allocator(None, None)
+    with pytest.raises(ValueError):
+        A.set_device_allocator(lambda n: 0, None)

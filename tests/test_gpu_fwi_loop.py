@@ -11,11 +11,13 @@
 * The reference's own order -- a gradient, step search and update per shot,
   with the last shot's trial misfit (fwi_run's defaults) or the all-shot sum --
   follows the same restatement to the same bounds.
+* A run continued from its resume file equals an uninterrupted one.
 """
 import numpy as np
 import pytest
 
 from conftest import rel_l2
+from cuda_fwi_gb300 import _capi
 from cuda_fwi_gb300 import problem as P
 from cuda_fwi_gb300.engine import Engine
 from oracle import fwi_loop as FL
@@ -128,3 +130,30 @@ def test_failed_search_retry_follows_restatement():
     assert [(a["trials"], a["status"]) for a in log] == [(b["trials"], b["status"]) for b in log_r] == [(14, 1)]
     assert log[0]["misfit"] == pytest.approx(log_r[0]["misfit"], rel=1e-4)
     assert np.array_equal(lam, p.lam) and np.array_equal(mu, p.mu) and np.array_equal(rho, p.rho)
+
+
+@pytest.mark.parametrize("order", ["summed", "per_shot"])
+def test_resume_file_continues_like_an_uninterrupted_run(order, tmp_path):
+    """fwi_psv_fwi_opts.resume_file: a run of one iteration saves the loop
+    state, a second run with max_iter 2 finds the file and does the second
+    iteration only; log and model equal an uninterrupted two-iteration run bit
+    for bit.  A file written under other options is refused."""
+    p, t, obs = _case()
+    kw = dict(max_iter=2, step_length=0.01, order=order, trial="sum", true_model=(t.lam, t.mu, t.rho))
+    with Engine(p) as eng:
+        eng.set_strategy("binomial", snapshots=8)
+        (lam_a, mu_a, rho_a), log_a = eng.fwi_run([0, 1], obs, **kw)
+    path = tmp_path / "fwi.resume"
+    with Engine(p) as eng:
+        eng.set_strategy("binomial", snapshots=8)
+        _, log_1 = eng.fwi_run([0, 1], obs, **dict(kw, max_iter=1), resume_file=path)
+    assert path.exists() and 1 <= len(log_1) <= len(log_a)
+    with Engine(p) as eng:  # a new engine: the state comes from the file
+        eng.set_strategy("binomial", snapshots=8)
+        (lam_b, mu_b, rho_b), log_b = eng.fwi_run([0, 1], obs, **kw, resume_file=path)
+        with pytest.raises(_capi.FwiError) as ei:
+            eng.fwi_run([0, 1], obs, **dict(kw, step_length=0.02), resume_file=path)
+        assert ei.value.code == "FWI_ERR_INVALID"
+    keys = ("misfit", "step_length", "trials", "status", "model_error")
+    assert [[r[k] for k in keys] for r in log_b] == [[r[k] for k in keys] for r in log_a]
+    assert np.array_equal(lam_b, lam_a) and np.array_equal(mu_b, mu_a) and np.array_equal(rho_b, rho_a)
