@@ -502,8 +502,9 @@ def main():
                        "longest nt, one launch per pass per order group, CUDA graphs; host wall clock over one "
                        "gradient of all models; the error column compares the first models with the one-model "
                        "engine running the same kernels on the same data (only the batching differs); per-model "
-                       "parity with the FP64 oracle is tests/test_gpu_multi.py (small models: records that miss "
-                       "the anomaly leave a near-zero residual, whose gradient is FP32 noise)"}
+                       "parity with the FP64 oracle: tests/test_gpu_multi.py (small models) and "
+                       "tests/test_gpu_fullsize.py (three of these models at their drawn sizes; models whose "
+                       "records miss the anomaly have a near-zero residual, whose gradient is FP32 noise)"}
 
     if rank == 0:
         out = {
