@@ -26,8 +26,9 @@ Cases:
   faulted layers, 32-slot binomial checkpointing.
 * Three models of the uneven batch (seed 4) at their drawn sizes, run together
   in the multi-model engine.
-* One shot of the FWI-loop workload, 2000x600 (2088x688), nt 5000: opt-in
-  (FWI_FULL_C5=1; a few minutes of host FP64 and ~10 GB of host memory).
+* One shot of the FWI-loop workload, 2000x600 (2088x688), nt 5000 (about
+  150 s, most of it host FP64, and ~10 GB of host memory; opt out with
+  FWI_SKIP_FULL_C5=1).
 
 Each test prints the measured errors.
 """
@@ -125,8 +126,8 @@ def test_config4_three_models_full_size():
                  float(mis[j]), grads[j], rows=rows[j], grid=_window_grid(p))
 
 
-@pytest.mark.skipif(os.environ.get("FWI_FULL_C5") != "1",
-                    reason="2000x600 nt 5000 single-shot parity (minutes of host FP64, ~10 GB); set FWI_FULL_C5=1")
+@pytest.mark.skipif(os.environ.get("FWI_SKIP_FULL_C5") == "1",
+                    reason="2000x600 nt 5000 single-shot parity skipped (FWI_SKIP_FULL_C5=1)")
 def test_config5_one_shot_full_size():
     true, syn = P.config5(True, nshots=96), P.config5(False, nshots=96)
     assert (syn.nzt, syn.nxt, syn.nt) == (688, 2088, 5000)
