@@ -128,9 +128,10 @@ enum {
  * the CPML (seismograms, misfit and residual as with the other strategies);
  * a second forward runs without CPML in a seeded random-velocity frame filling
  * the padding (velocities scaled by 1 - 0.5 (depth into the padding / ppad) u,
- * u uniform in [0, 1)); the backward rebuilds that second wavefield by undoing
- * its steps in reverse (FP32 round-off makes it drift slightly) and correlates
- * it with the adjoint wavefield, which keeps the CPML.  Cost per shot
+ * u uniform in [0, 1) per block of 16 x 16 cells); the backward rebuilds that
+ * second wavefield by undoing its steps in reverse (FP32 round-off makes it
+ * drift slightly) and correlates it with the adjoint wavefield, which keeps
+ * the CPML.  Cost per shot
  * gradient: 4 nt time steps (the frame forward and the reverse sweep count as
  * recompute_steps).  Needs the TMA mapping (the default), no free surface (its
  * surface row is assigned, not incremented, so it cannot be undone) and

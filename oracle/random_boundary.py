@@ -14,8 +14,9 @@ on the frame materials for the storage, then orc_adjoint with the real CPML
 and medium.
 
 The frame: in the padding, velocities are scaled by f = 1 - alpha (d / ppad) u
-with d the depth into the padding and u = (hash(cell) >> 8) / 2^24, the same
-hash the engine uses; lam, mu and mu_zx are scaled by f^2, densities kept.
+with d the depth into the padding and u = (hash(block) >> 8) / 2^24 per block
+of GRAIN x GRAIN cells, the same hash the engine uses; lam, mu and mu_zx are
+scaled by f^2, densities kept.
 """
 from __future__ import annotations
 
@@ -27,6 +28,7 @@ from . import oracle as O
 
 SEED = 20090625
 ALPHA = np.float32(0.5)
+GRAIN = 16
 M32 = 0xFFFFFFFF
 
 
@@ -49,8 +51,8 @@ def frame_factor2(p):
     if not p.fsurf:
         d = np.maximum(d, p.ppad - iz)
     d = np.maximum(d, iz - (p.nzt - 1 - p.ppad))
-    i = (iz * p.nxt + ix).astype(np.uint64)
-    h = _hash_u32((i * np.uint64(2654435761) + np.uint64(SEED)) & np.uint64(M32))
+    key = ((iz // GRAIN) * 65599 + (ix // GRAIN)).astype(np.uint64) & np.uint64(M32)
+    h = _hash_u32((key * np.uint64(2654435761) + np.uint64(SEED)) & np.uint64(M32))
     u = (h >> np.uint64(8)).astype(np.float32) * np.float32(1.0 / 16777216.0)
     q = d.astype(np.float32) / np.float32(max(p.ppad, 1))
     f = np.float32(1.0) - ALPHA * q * u
