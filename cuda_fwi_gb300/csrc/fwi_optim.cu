@@ -387,8 +387,13 @@ static int resume_load(const char* path, const fwi_psv_fwi_opts* o, size_t cells
     *found = false;
     FILE* f = std::fopen(path, "rb");
     if (!f) return FWI_OK;
-    bool ok = std::fread(h, sizeof(*h), 1, f) == 1 && resume_matches(*h, o, cells, nshots) &&
-              h->entries <= capacity;
+    bool ok = std::fread(h, sizeof(*h), 1, f) == 1 && resume_matches(*h, o, cells, nshots);
+    if (ok && h->entries > capacity) {
+        std::fclose(f);
+        return fwi::fail(FWI_ERR_INVALID, std::string("the resume file ") + path + " holds " +
+                                              std::to_string(h->entries) + " log entries, more than max_iter allows (" +
+                                              std::to_string(capacity) + ")");
+    }
     if (ok && h->entries > 0) ok = std::fread(log, sizeof(fwi_psv_fwi_iter), h->entries, f) == (size_t)h->entries;
     for (int q = 0; q < 3 && ok; q++) {
         model[q].resize(cells);
