@@ -750,9 +750,8 @@ __device__ __forceinline__ unsigned atom_add_acq_rel_cta(unsigned* p, unsigned v
 }
 
 template <int FP, int STAGE_FLOATS, bool NEXT = false, class Coords, class Issue, class Compute>
-__device__ __forceinline__ void tma_pipeline(int ntiles, int* err, Coords coords, Issue issue,
-                                                   Compute compute, unsigned long long wait_ns = 0,
-                                                   int stall = 0) {
+__device__ __forceinline__ void tma_pipeline(int ntiles, int* err, Coords coords, Issue issue, Compute compute,
+                                             unsigned long long wait_ns = 0, int stall = 0) {
     constexpr int S = stages_for<STAGE_FLOATS>();
     const unsigned long long lim = wait_ns ? wait_ns : kWaitNs;
     static_assert(STAGE_FLOATS % 32 == 0, "stages are 128-byte multiples");
@@ -765,8 +764,11 @@ __device__ __forceinline__ void tma_pipeline(int ntiles, int* err, Coords coords
     volatile int* abort = reinterpret_cast<volatile int*>(issued + S);
     const int tid = threadIdx.x, lane = tid & 31;
     const unsigned nwarps = blockDim.x >> 5;
+    // an earlier launch gave up (error word set): return at once, so a failing
+    // pipeline costs one bounded wait and not one per launch; the decision is
+    // CTA-uniform (every thread reaches the barrier)
     if (__syncthreads_or(*(volatile int*)err != 0)) return;
-    if (smem_u32(tma_smem) & 127u) {
+    if (smem_u32(tma_smem) & 127u) {  // TMA destinations need 128-byte alignment
         if (tid == 0) atomicOr(err, 8);
         return;
     }
