@@ -410,6 +410,11 @@ __device__ __forceinline__ void stress_rows(const ItemDesc& D, const float* st, 
     float mx1[R][2], mx2[R][2];
     float2 mz1[R], mz2[R];
     int pzr[R];
+    // z-strip coefficients loaded with the memories before the row loop (inside
+    // it their loads wait behind the previous row's CPML stores); above half
+    // order 4, per row, as held across the rows they cost spills
+    constexpr bool kHoistCz = FP <= 4;
+    Cpml czr[R];
     int xf[2] = {-1, -1};
     if constexpr (!INTERIOR) {
 #pragma unroll
@@ -428,6 +433,7 @@ __device__ __forceinline__ void stress_rows(const ItemDesc& D, const float* st, 
             if (pzr[rr] >= 0) {
                 mz1[rr] = ld2(mvz_z + msrc + (size_t)pzr[rr] * P + ix);
                 mz2[rr] = ld2(mvx_z + msrc + (size_t)pzr[rr] * P + ix);
+                if constexpr (kHoistCz) czr[rr] = load_cpml6(D.cpml, tp, pzr[rr]);
             }
         }
         // sampled window columns (forward storage for the gradient)
@@ -466,7 +472,9 @@ __device__ __forceinline__ void stress_rows(const ItemDesc& D, const float* st, 
         if constexpr (!INTERIOR) {
             cpml_x_pair(pc, D.cpml, iz, tp, mx1[rr], mx2[rr], mvx_x, mvz_x, vx_x, vz_x);
             if (pzr[rr] >= 0) {
-                const Cpml cz = load_cpml6(D.cpml, tp, pzr[rr]);
+                Cpml cz;
+                if constexpr (kHoistCz) cz = czr[rr];
+                else cz = load_cpml6(D.cpml, tp, pzr[rr]);
                 const size_t m = (size_t)pzr[rr] * P + ix;
                 const float2 m1 = fma2(bc2(cz.b), mz1[rr], mul2(bc2(cz.a), vz_z));
                 const float2 m2 = fma2(bc2(cz.bh), mz2[rr], mul2(bc2(cz.ah), vx_z));
@@ -616,6 +624,9 @@ __device__ __forceinline__ void velocity_rows(const ItemDesc& D, const float* st
     // them); above, per row, as held across the rows they cost spills
     constexpr bool kHoistCx = FP <= 4;
     Cpml cx[2];
+    // z-strip coefficients likewise (as in the stress pass)
+    constexpr bool kHoistCz = FP <= 4;
+    Cpml czr[R];
     if constexpr (!INTERIOR) {
         if constexpr (kHoistCx) load_cpml_x(pc, D.cpml, tp, cx);
 #pragma unroll
@@ -634,6 +645,7 @@ __device__ __forceinline__ void velocity_rows(const ItemDesc& D, const float* st
             if (pzr[rr] >= 0) {
                 mz1[rr] = ld2(mszz_z + msrc + (size_t)pzr[rr] * P + ix);
                 mz2[rr] = ld2(mszx_z + msrc + (size_t)pzr[rr] * P + ix);
+                if constexpr (kHoistCz) czr[rr] = load_cpml6(D.cpml, tp, pzr[rr]);
             }
         }
     }
@@ -663,7 +675,9 @@ __device__ __forceinline__ void velocity_rows(const ItemDesc& D, const float* st
             if constexpr (kHoistCx) cpml_x_pair(pc, cx, iz, tp, mx1[rr], mx2[rr], msxx_x, mszx_x, sxx_x, szx_x);
             else cpml_x_pair(pc, D.cpml, iz, tp, mx1[rr], mx2[rr], msxx_x, mszx_x, sxx_x, szx_x);
             if (pzr[rr] >= 0) {
-                const Cpml cz = load_cpml6(D.cpml, tp, pzr[rr]);
+                Cpml cz;
+                if constexpr (kHoistCz) cz = czr[rr];
+                else cz = load_cpml6(D.cpml, tp, pzr[rr]);
                 const size_t m = (size_t)pzr[rr] * P + ix;
                 const float2 m1 = fma2(bc2(cz.b), mz1[rr], mul2(bc2(cz.a), szz_z));
                 const float2 m2 = fma2(bc2(cz.bh), mz2[rr], mul2(bc2(cz.ah), szx_z));
