@@ -1060,10 +1060,14 @@ __device__ __forceinline__ void adjoint_rows(const ItemDesc& D, const float* st,
             }
         }
     }
-    // CPML memories of the pair
+    // CPML memories of the pair, and the z-strip coefficients of its row (up
+    // to half order 4: loaded here, not after the stencil where the load
+    // would sit on the update's path)
     float mx1[2] = {0.f, 0.f}, mx2[2] = {0.f, 0.f};
     float2 mz1 = make_float2(0.f, 0.f), mz2 = make_float2(0.f, 0.f);
     int pz = -1;
+    constexpr bool kHoistCz = FP <= 4;
+    Cpml cz0;
     if constexpr (!INTERIOR) {
 #pragma unroll
         for (int l = 0; l < 2; l++) {
@@ -1076,6 +1080,7 @@ __device__ __forceinline__ void adjoint_rows(const ItemDesc& D, const float* st,
         if (pz >= 0) {
             mz1 = ld2(D.mvz_z + (size_t)pz * P + ix);
             mz2 = ld2(D.mvx_z + (size_t)pz * P + ix);
+            if constexpr (kHoistCz) cz0 = load_cpml6(D.cpml, tp, pz);
         }
     }
     const float* svx = st;
@@ -1103,7 +1108,9 @@ __device__ __forceinline__ void adjoint_rows(const ItemDesc& D, const float* st,
     if constexpr (!INTERIOR) {
         cpml_x_pair(pc, D.cpml, iz, tp, mx1, mx2, D.mvx_x, D.mvz_x, vx_x, vz_x);
         if (pz >= 0) {
-            const Cpml cz = load_cpml6(D.cpml, tp, pz);
+            Cpml cz;
+            if constexpr (kHoistCz) cz = cz0;
+            else cz = load_cpml6(D.cpml, tp, pz);
             const size_t m = (size_t)pz * P + ix;
             const float2 m1 = fma2(bc2(cz.b), mz1, mul2(bc2(cz.a), vz_z));
             const float2 m2 = fma2(bc2(cz.bh), mz2, mul2(bc2(cz.ah), vx_z));
