@@ -3,7 +3,8 @@
 Each model's misfit and reference gradient against the FP64 oracle run on
 that model alone (relative L2: misfit 1e-4, gradients 1e-4); graph replay and
 direct launches agree bitwise; the autotuner writes its choices to the JSON
-cache and a second engine reads them back.
+cache and a second engine reads them back; a forward runs the mappings a
+gradient runs.
 """
 import json
 
@@ -116,3 +117,19 @@ def test_tma_tiles_match_oracle(tune_cache):
         for i in range(3):
             assert rel_l2(grads[k][i], _oracle_grid(p, g_o[i])) <= 1e-4, (k, i)
             assert np.array_equal(grads[k][i], grads_r[k][i])
+
+
+def test_forward_uses_the_gradients_mappings(tune_cache):
+    """A forward tunes like a gradient (or reads the same cache), so every
+    engine over the same models computes the same traces bit for bit, with the
+    choices forced to the TMA tiles or left to the tuner."""
+    ps, obs = _models()
+    with MultiEngine(ps, snapshots=4, autotune=True) as m:
+        m.gradient(obs)
+        rec_a = m.forward()
+    with MultiEngine(ps, snapshots=4, autotune=True) as m:
+        rec_b = m.forward()  # no gradient first: the cache written above
+        tun = m.tuning()
+    assert all(t["cached"] for t in tun)
+    for a, b in zip(rec_a, rec_b):
+        assert np.array_equal(a, b)
