@@ -645,6 +645,22 @@ struct DBuf {
 
 static size_t round_up(size_t v, size_t m) { return (v + m - 1) / m * m; }
 
+// Bounds-checked build (FWI_BOUNDS_CHECK): the first out-of-range access a
+// kernel recorded since the last call, reported and cleared.
+static int check_bounds_record() {
+#if FWI_BOUNDS_CHECK
+    unsigned long long v = 0;
+    CUDA_TRY(cudaMemcpyFromSymbol(&v, g_fwi_oob, sizeof(v)));
+    if (v) {
+        const unsigned long long zero = 0;
+        CUDA_TRY(cudaMemcpyToSymbol(g_fwi_oob, &zero, sizeof(zero)));
+        return fail(FWI_ERR_CUDA, "out-of-range index " + std::to_string((long long)(v & 0xFFFFFFFFFFFFull)) +
+                                      " at access site " + std::to_string((int)(v >> 48)) + "; results discarded");
+    }
+#endif
+    return FWI_OK;
+}
+
 // page-locked host staging buffer (fast, asynchronous copies)
 struct HBuf {
     void* p = nullptr;
@@ -1617,6 +1633,7 @@ struct Engine {
     // Error flags raised by the kernels: bit 4 a bounded wait that ran out
     // (bit 8 misaligned shared memory), bit 16 the watchdog's non-finite values.
     int check_kernel_flags() {
+        FWI_TRY(check_bounds_record());
         int h = 0;
         CUDA_TRY(cudaMemcpy(&h, d_err.p, sizeof(int), cudaMemcpyDeviceToHost));
         if (h) {

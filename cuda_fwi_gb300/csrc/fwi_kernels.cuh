@@ -89,6 +89,37 @@ struct Cpml {
     float a, b, iK, ah, bh, iKh;
 };
 
+// Bounds-checked debug build (-DFWI_BOUNDS_CHECK=1; compute-sanitizer is not
+// available on every GPU host).  inb(i, n, site) guards an access to element i
+// of an n-element array: in the checked build an index outside [0, n) records
+// the first offending (site, index) in g_fwi_oob and the access is skipped, no
+// trap; in the normal build it is true and compiles away.  The engine reads
+// the record after each call (FWI_ERR_CUDA "out-of-range index").  Sites:
+// 1x forward stress pass, 2x forward velocity pass, 3x adjoint stress pass
+// (TMA-staged kernels).
+#ifndef FWI_BOUNDS_CHECK
+#define FWI_BOUNDS_CHECK 0
+#endif
+#if FWI_BOUNDS_CHECK
+static __device__ unsigned long long g_fwi_oob;  // site << 48 | index (low 48 bits)
+#endif
+__device__ __forceinline__ bool inb(long long i, long long n, int site) {
+#if FWI_BOUNDS_CHECK
+    if (i >= 0 && i < n) return true;
+    atomicCAS(&g_fwi_oob, 0ull, ((unsigned long long)site << 48) | ((unsigned long long)i & 0xFFFFFFFFFFFFull));
+    return false;
+#else
+    (void)i, (void)n, (void)site;
+    return true;
+#endif
+}
+// Element counts of a slot's arrays: fields [nzt][pitch], x-strip memories
+// [nzt][tp], z-strip memories [tp][pitch], gradients [nfz][nfx].
+#define FWI_NFIELD(D) ((long long)(D).nzt * (D).pitch)
+#define FWI_NXS(D) ((long long)(D).nzt * (D).tp)
+#define FWI_NZS(D) ((long long)(D).tp * (D).pitch)
+#define FWI_NGRAD(D) ((long long)(D).nfz * (D).nfx)
+
 __device__ __forceinline__ Cpml load_cpml(const float* __restrict__ c, int tp, int p) {
     Cpml r;
     r.a = __ldg(c + p);

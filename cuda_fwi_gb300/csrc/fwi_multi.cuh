@@ -873,6 +873,7 @@ struct MultiEngine {
         CUDA_TRY(cudaMemcpyAsync(h.data(), d_rec.p, total_rec * 4, cudaMemcpyDeviceToHost, stream));
         CUDA_TRY(cudaStreamSynchronize(stream));
         int flag = 0;
+        FWI_TRY(check_bounds_record());
         CUDA_TRY(cudaMemcpy(&flag, d_err.p, 4, cudaMemcpyDeviceToHost));
         if (flag) return fail(FWI_ERR_CUDA, "a kernel raised its error flag; results discarded");
         for (int b = 0; b < n; b++)
@@ -1030,6 +1031,7 @@ struct MultiEngine {
         if (want_g) CUDA_TRY(cudaMemcpyAsync(g.data(), d_grad.p, total_grad * 4, cudaMemcpyDeviceToHost, stream));
         CUDA_TRY(cudaStreamSynchronize(stream));
         int flag = 0;
+        FWI_TRY(check_bounds_record());
         CUDA_TRY(cudaMemcpy(&flag, d_err.p, 4, cudaMemcpyDeviceToHost));
         float ms = 0.f;
         cudaEventElapsedTime(&ms, e0, e1);

@@ -314,7 +314,7 @@ __device__ __forceinline__ void cpml_x_pair(const PairCols& pc, const float* __r
                                             float* __restrict__ a2, float2& d1, float2& d2) {
 #pragma unroll
     for (int l = 0; l < 2; l++)
-        if (pc.px[l] >= 0)
+        if (pc.px[l] >= 0 && inb(pc.px[l], tp, 1))
             cpml_x_lane(load_cpml6(cpml, tp, pc.px[l]), (size_t)iz * tp + pc.px[l], o1[l], o2[l], a1, a2,
                         l ? d1.y : d1.x, l ? d2.y : d2.x);
 }
@@ -324,7 +324,7 @@ __device__ __forceinline__ void load_cpml_x(const PairCols& pc, const float* __r
                                             Cpml (&cx)[2]) {
 #pragma unroll
     for (int l = 0; l < 2; l++)
-        if (pc.px[l] >= 0) cx[l] = load_cpml6(cpml, tp, pc.px[l]);
+        if (pc.px[l] >= 0 && inb(pc.px[l], tp, 21)) cx[l] = load_cpml6(cpml, tp, pc.px[l]);
 }
 __device__ __forceinline__ void cpml_x_pair(const PairCols& pc, const Cpml (&cx)[2], int iz, int tp,
                                             const float (&o1)[2], const float (&o2)[2], float* __restrict__ a1,
@@ -424,12 +424,14 @@ __device__ __forceinline__ void stress_rows(const ItemDesc& D, const float* st, 
 #pragma unroll
             for (int l = 0; l < 2; l++) {
                 mx1[rr][l] = mx2[rr][l] = 0.f;
-                if (pc.px[l] >= 0 && iz < nzt - FP) {
+                if (pc.px[l] >= 0 && iz < nzt - FP && inb((long long)iz * tp + pc.px[l], FWI_NXS(D), 11)) {
                     mx1[rr][l] = (mvx_x + msrc)[(size_t)iz * tp + pc.px[l]];
                     mx2[rr][l] = (mvz_x + msrc)[(size_t)iz * tp + pc.px[l]];
                 }
             }
             pzr[rr] = strip_z<FP>(D, iz, true);
+            if (pzr[rr] >= 0 && !(inb(pzr[rr], tp, 12) && inb((long long)pzr[rr] * P + ix + 1, FWI_NZS(D), 12)))
+                pzr[rr] = -1;
             if (pzr[rr] >= 0) {
                 mz1[rr] = ld2(mvz_z + msrc + (size_t)pzr[rr] * P + ix);
                 mz2[rr] = ld2(mvx_z + msrc + (size_t)pzr[rr] * P + ix);
@@ -490,10 +492,13 @@ __device__ __forceinline__ void stress_rows(const ItemDesc& D, const float* st, 
         if constexpr (!INTERIOR) {
             if ((xf[0] >= 0 || xf[1] >= 0) && iz >= D.wz1 && iz < D.wz2 && (iz - D.wz1) % D.fwi_dz == 0) {
                 const size_t fs = (size_t)D.nfz * D.nfx;
-                float* s = D.store + (size_t)(it / D.fwi_dt) * 5 * fs + (size_t)((iz - D.wz1) / D.fwi_dz) * D.nfx;
+                const size_t so = (size_t)(it / D.fwi_dt) * 5 * fs + (size_t)((iz - D.wz1) / D.fwi_dz) * D.nfx;
+                float* s = D.store + so;
 #pragma unroll
                 for (int l = 0; l < 2; l++) {
-                    if (xf[l] < 0) continue;
+                    if (xf[l] < 0 ||
+                        !inb((long long)(so + xf[l] + 4 * fs), (long long)(1 + (D.nt - 1) / D.fwi_dt) * 5 * fs, 14))
+                        continue;
                     float* q = s + xf[l];
                     q[F_VX * fs] = lane(wvx[rr + FP - 1], l) / D.dt;
                     q[F_VZ * fs] = lane(wvz[rr + FP], l) / D.dt;
@@ -507,6 +512,7 @@ __device__ __forceinline__ void stress_rows(const ItemDesc& D, const float* st, 
         const float2 tr = mul2(L, add2(vx_x, vz_z));
         sxx = fma2(sg, fma2(M2, vx_x, tr), sxx);
         szz = fma2(sg, fma2(M2, vz_z, tr), szz);
+        if (!inb((long long)c + 1, FWI_NFIELD(D), 13)) continue;
         if constexpr (INTERIOR) {
             *reinterpret_cast<float2*>(gsxx + c) = sxx;
             *reinterpret_cast<float2*>(gszx + c) = szx;
@@ -636,12 +642,14 @@ __device__ __forceinline__ void velocity_rows(const ItemDesc& D, const float* st
 #pragma unroll
             for (int l = 0; l < 2; l++) {
                 mx1[rr][l] = mx2[rr][l] = 0.f;
-                if (pc.px[l] >= 0 && iz < nzt - FP) {
+                if (pc.px[l] >= 0 && iz < nzt - FP && inb((long long)iz * tp + pc.px[l], FWI_NXS(D), 22)) {
                     mx1[rr][l] = (msxx_x + msrc)[(size_t)iz * tp + pc.px[l]];
                     mx2[rr][l] = (mszx_x + msrc)[(size_t)iz * tp + pc.px[l]];
                 }
             }
             pzr[rr] = strip_z<FP>(D, iz, false);
+            if (pzr[rr] >= 0 && !(inb(pzr[rr], tp, 23) && inb((long long)pzr[rr] * P + ix + 1, FWI_NZS(D), 23)))
+                pzr[rr] = -1;
             if (pzr[rr] >= 0) {
                 mz1[rr] = ld2(mszz_z + msrc + (size_t)pzr[rr] * P + ix);
                 mz2[rr] = ld2(mszx_z + msrc + (size_t)pzr[rr] * P + ix);
@@ -690,6 +698,7 @@ __device__ __forceinline__ void velocity_rows(const ItemDesc& D, const float* st
         const int ci = r * kTmaTX + cp;
         const float2 vxn = fma2(sg, mul2(ld2(cen + ci), add2(sxx_x, szx_z)), ld2(cen + 2 * G::CEN + ci));
         const float2 vzn = fma2(sg, mul2(ld2(cen + G::CEN + ci), add2(szx_x, szz_z)), ld2(cen + 3 * G::CEN + ci));
+        if (!inb((long long)c + 1, FWI_NFIELD(D), 24)) continue;
         if constexpr (INTERIOR) {
             if (we)
                 *reinterpret_cast<float2*>(gwe + c) = add2(ld2(cen + 4 * G::CEN + ci), fma2(vxn, vxn, mul2(vzn, vzn)));
@@ -1042,6 +1051,9 @@ __device__ __forceinline__ void adjoint_rows(const ItemDesc& D, const float* st,
                 }
             }
         }
+#pragma unroll
+        for (int l = 0; l < 2; l++)
+            if ((INTERIOR || gi[l] >= 0) && !inb(gi[l], FWI_NGRAD(D), 31)) gi[l] = -2;  // -2: skipped
         if (INTERIOR && ga.valid) {
 #pragma unroll
             for (int l = 0; l < 2; l++) {
@@ -1071,12 +1083,13 @@ __device__ __forceinline__ void adjoint_rows(const ItemDesc& D, const float* st,
     if constexpr (!INTERIOR) {
 #pragma unroll
         for (int l = 0; l < 2; l++) {
-            if (pc.px[l] >= 0) {
+            if (pc.px[l] >= 0 && inb((long long)iz * tp + pc.px[l], FWI_NXS(D), 33)) {
                 mx1[l] = D.mvx_x[(size_t)iz * tp + pc.px[l]];
                 mx2[l] = D.mvz_x[(size_t)iz * tp + pc.px[l]];
             }
         }
         pz = strip_z<FP>(D, iz, true);
+        if (pz >= 0 && !(inb(pz, tp, 34) && inb((long long)pz * P + ix + 1, FWI_NZS(D), 34))) pz = -1;
         if (pz >= 0) {
             mz1 = ld2(D.mvz_z + (size_t)pz * P + ix);
             mz2 = ld2(D.mvx_z + (size_t)pz * P + ix);
@@ -1148,7 +1161,7 @@ __device__ __forceinline__ void adjoint_rows(const ItemDesc& D, const float* st,
         const float2 nr = fma2(make_float2(-D.gscale, -D.gscale), s4, make_float2(g2[0], g2[1]));
 #pragma unroll
         for (int l = 0; l < 2; l++) {
-            if (INTERIOR || gi[l] >= 0) {
+            if ((INTERIOR && (!FWI_BOUNDS_CHECK || gi[l] != -2)) || gi[l] >= 0) {
                 glam[gi[l]] = lane(nl, l);
                 gmu[gi[l]] = lane(nm, l);
                 grho[gi[l]] = lane(nr, l);
@@ -1159,6 +1172,7 @@ __device__ __forceinline__ void adjoint_rows(const ItemDesc& D, const float* st,
     const float2 tr = mul2(L, add2(vx_x, vz_z));
     sxx = add2(sxx, fma2(M2, vx_x, tr));
     szz = add2(szz, fma2(M2, vz_z, tr));
+    if (!inb((long long)c + 1, FWI_NFIELD(D), 35)) return;
     if constexpr (INTERIOR) {
         *reinterpret_cast<float2*>(D.ux + c) = ux;
         *reinterpret_cast<float2*>(D.uz + c) = uz;
@@ -1221,6 +1235,7 @@ __global__ void __launch_bounds__(kAdjThreads, 1)
             if (grad && n.x >= 0 && interior_warp_adj(g, n.y, n.z, true, ln)) {
                 const ItemDesc* In = items + n.x;
                 const int gi = (n.z + ln / (kTmaTX / 2) - wz1) * nfx + (n.y + (ln & (kTmaTX / 2 - 1)) * 2 - wx1);
+                if (!inb((long long)gi + 1, (long long)__ldg(&In->nfz) * nfx, 36)) return;
                 const float* gl = ldg_ptr(&In->glam);
                 const float* gm = ldg_ptr(&In->gmu);
                 const float* gr = ldg_ptr(&In->grho);
