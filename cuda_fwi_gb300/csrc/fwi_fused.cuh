@@ -118,7 +118,7 @@ __device__ __forceinline__ void cpml_x_pair_own(const PairCols& pc, const float*
                                                 float* __restrict__ a2, float2& d1, float2& d2, bool own) {
 #pragma unroll
     for (int l = 0; l < 2; l++)
-        if (pc.px[l] >= 0)
+        if (pc.px[l] >= 0 && inb(pc.px[l], tp, 41))
             cpml_x_lane(load_cpml6(cpml, tp, pc.px[l]), (size_t)iz * tp + pc.px[l], o1[l], o2[l], a1, a2,
                         l ? d1.y : d1.x, l ? d2.y : d2.x, own);
 }
@@ -218,12 +218,14 @@ __device__ __forceinline__ void fused_stress(const ItemDesc& D, const float* st,
 #pragma unroll
             for (int l = 0; l < 2; l++) {
                 mx1[rr][l] = mx2[rr][l] = 0.f;
-                if (pc.px[l] >= 0 && iz < nzt - FP) {
+                if (pc.px[l] >= 0 && iz < nzt - FP && inb((long long)iz * tp + pc.px[l], FWI_NXS(D), 42)) {
                     mx1[rr][l] = (mvx_x + msrc)[(size_t)iz * tp + pc.px[l]];
                     mx2[rr][l] = (mvz_x + msrc)[(size_t)iz * tp + pc.px[l]];
                 }
             }
             pzr[rr] = strip_z<FP>(D, iz, true);
+            if (pzr[rr] >= 0 && !(inb(pzr[rr], tp, 43) && inb((long long)pzr[rr] * P + ix + 1, FWI_NZS(D), 43)))
+                pzr[rr] = -1;
             if (pzr[rr] >= 0) {
                 mz1[rr] = ld2(mvz_z + msrc + (size_t)pzr[rr] * P + ix);
                 mz2[rr] = ld2(mvx_z + msrc + (size_t)pzr[rr] * P + ix);
@@ -287,10 +289,13 @@ __device__ __forceinline__ void fused_stress(const ItemDesc& D, const float* st,
         if constexpr (!INTERIOR) {
             if ((xf[0] >= 0 || xf[1] >= 0) && iz >= D.wz1 && iz < D.wz2 && (iz - D.wz1) % D.fwi_dz == 0) {
                 const size_t fs = (size_t)D.nfz * D.nfx;
-                float* s = D.store + (size_t)(it / D.fwi_dt) * 5 * fs + (size_t)((iz - D.wz1) / D.fwi_dz) * D.nfx;
+                const size_t so = (size_t)(it / D.fwi_dt) * 5 * fs + (size_t)((iz - D.wz1) / D.fwi_dz) * D.nfx;
+                float* s = D.store + so;
 #pragma unroll
                 for (int l = 0; l < 2; l++) {
-                    if (xf[l] < 0) continue;
+                    if (xf[l] < 0 ||
+                        !inb((long long)(so + xf[l] + 4 * fs), (long long)(1 + (D.nt - 1) / D.fwi_dt) * 5 * fs, 44))
+                        continue;
                     float* q = s + xf[l];
                     q[F_VX * fs] = lane(wvx[rr + FP - 1], l) / D.dt;
                     q[F_VZ * fs] = lane(wvz[rr + FP], l) / D.dt;
@@ -304,8 +309,10 @@ __device__ __forceinline__ void fused_stress(const ItemDesc& D, const float* st,
         const float2 tr = mul2(L, add2(vx_x, vz_z));
         sxx = fma2(sg, fma2(M2, vx_x, tr), sxx);
         szz = fma2(sg, fma2(M2, vz_z, tr), szz);
+        // global stores only where the index is in range (the ring below always)
+        const bool gok = inb((long long)c + 1, FWI_NFIELD(D), 45);
         if constexpr (INTERIOR) {
-            if (own) {
+            if (own && gok) {
                 *reinterpret_cast<float2*>(gsxx + c) = sxx;
                 *reinterpret_cast<float2*>(gszx + c) = szx;
                 *reinterpret_cast<float2*>(gszz + c) = szz;
@@ -320,17 +327,18 @@ __device__ __forceinline__ void fused_stress(const ItemDesc& D, const float* st,
                 sxx.x = fsurf_sxx(vx_x.x, L.x, M2.x);
                 sxx.y = fsurf_sxx(vx_x.y, L.y, M2.y);
             }
-            st2(gsxx + c, sxx, pc.on0 && own, pc.on1 && own);
-            st2(gszx + c, szx, pc.on0 && own, pc.on1 && own);
-            st2(gszz + c, szz, pc.on0 && own, pc.on1 && own);
+            st2(gsxx + c, sxx, pc.on0 && own && gok, pc.on1 && own && gok);
+            st2(gszx + c, szx, pc.on0 && own && gok, pc.on1 && own && gok);
+            st2(gszz + c, szz, pc.on0 && own && gok, pc.on1 && own && gok);
             *reinterpret_cast<float2*>(nsxx + o) = masked(sxx, pc);
             *reinterpret_cast<float2*>(nszx + o) = masked(szx, pc);
             *reinterpret_cast<float2*>(nszz + o) = masked(szz, pc);
             if (fsurf && iz > FP && iz <= 2 * FP) {
                 const size_t cm = (size_t)(2 * FP - iz) * P + ix;
                 const float2 mx = make_float2(-szx.x, -szx.y), mzz = make_float2(-szz.x, -szz.y);
-                st2(gszx + cm, mx, pc.on0 && own, pc.on1 && own);
-                st2(gszz + cm, mzz, pc.on0 && own, pc.on1 && own);
+                const bool mok = inb((long long)cm + 1, FWI_NFIELD(D), 46);
+                st2(gszx + cm, mx, pc.on0 && own && mok, pc.on1 && own && mok);
+                st2(gszz + cm, mzz, pc.on0 && own && mok, pc.on1 && own && mok);
                 // ring row of the mirror row 2FP - iz (head rows of a unit's first chunk)
                 const int om = (2 * FP - iz - (z - 2 * FP)) * G::SX + cs;
                 *reinterpret_cast<float2*>(nszx + om) = masked(mx, pc);
@@ -398,12 +406,15 @@ __device__ __forceinline__ void fused_velocity(const ItemDesc& D, const float* s
 #pragma unroll
             for (int l = 0; l < 2; l++) {
                 mx1[rr][l] = mx2[rr][l] = 0.f;
-                if (pc.px[l] >= 0 && iz >= FP && iz < nzt - FP) {
+                if (pc.px[l] >= 0 && iz >= FP && iz < nzt - FP &&
+                    inb((long long)iz * tp + pc.px[l], FWI_NXS(D), 47)) {
                     mx1[rr][l] = (msxx_x + msrc)[(size_t)iz * tp + pc.px[l]];
                     mx2[rr][l] = (mszx_x + msrc)[(size_t)iz * tp + pc.px[l]];
                 }
             }
             pzr[rr] = iz >= FP ? strip_z<FP>(D, iz, false) : -1;
+            if (pzr[rr] >= 0 && !(inb(pzr[rr], tp, 48) && inb((long long)pzr[rr] * P + ix + 1, FWI_NZS(D), 48)))
+                pzr[rr] = -1;
             if (pzr[rr] >= 0) {
                 mz1[rr] = ld2(mszz_z + msrc + (size_t)pzr[rr] * P + ix);
                 mz2[rr] = ld2(mszx_z + msrc + (size_t)pzr[rr] * P + ix);
@@ -451,6 +462,7 @@ __device__ __forceinline__ void fused_velocity(const ItemDesc& D, const float* s
         const float2 vxo = ld2(svx + q * G::VX + vcol), vzo = ld2(svz + q * G::VX + vcol);
         const float2 vxn = fma2(sg, mul2(ld2(sbx + bi), add2(sxx_x, szx_z)), vxo);
         const float2 vzn = fma2(sg, mul2(ld2(sbz + bi), add2(szx_x, szz_z)), vzo);
+        if (!inb((long long)c + 1, FWI_NFIELD(D), 49)) continue;
         if constexpr (INTERIOR) {
             if (we) *reinterpret_cast<float2*>(gwe + c) = add2(ld2(gwe + c), fma2(vxn, vxn, mul2(vzn, vzn)));
             *reinterpret_cast<float2*>(gvx + c) = vxn;

@@ -94,9 +94,10 @@ struct Cpml {
 // of an n-element array: in the checked build an index outside [0, n) records
 // the first offending (site, index) in g_fwi_oob and the access is skipped, no
 // trap; in the normal build it is true and compiles away.  The engine reads
-// the record after each call (FWI_ERR_CUDA "out-of-range index").  Sites:
-// 1x forward stress pass, 2x forward velocity pass, 3x adjoint stress pass
-// (TMA-staged kernels).
+// the record after each call (FWI_ERR_CUDA "out-of-range index").  Sites of
+// the TMA-staged kernels: 1-2 x-strip CPML of a pair, 11-14 forward stress
+// pass, 21-24 forward velocity pass, 31-36 adjoint stress pass, 41-49 fused
+// forward step.  The cell mappings and the exact adjoint are not guarded.
 #ifndef FWI_BOUNDS_CHECK
 #define FWI_BOUNDS_CHECK 0
 #endif

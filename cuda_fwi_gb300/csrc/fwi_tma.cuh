@@ -331,7 +331,7 @@ __device__ __forceinline__ void cpml_x_pair(const PairCols& pc, const Cpml (&cx)
                                             float* __restrict__ a2, float2& d1, float2& d2) {
 #pragma unroll
     for (int l = 0; l < 2; l++)
-        if (pc.px[l] >= 0)
+        if (pc.px[l] >= 0 && inb(pc.px[l], tp, 2))
             cpml_x_lane(cx[l], (size_t)iz * tp + pc.px[l], o1[l], o2[l], a1, a2, l ? d1.y : d1.x, l ? d2.y : d2.x);
 }
 

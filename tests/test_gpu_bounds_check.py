@@ -1,8 +1,9 @@
 """The bounds-checked debug build (-DFWI_BOUNDS_CHECK=1) on valid inputs.
 
 compute-sanitizer is not available on every GPU host; in the checked build the
-TMA-staged passes guard their global-memory accesses (fields, CPML memories,
-gradients, storage; see `inb` in csrc/fwi_kernels.cuh), recording the first
+TMA-staged passes and the fused step guard their global-memory accesses
+(fields, CPML memories, gradients, storage; see `inb` in
+csrc/fwi_kernels.cuh), recording the first
 out-of-range access, skipping it, and making the call fail.  On these valid
 cases the checked library must record nothing and give the normal library's
 results bit for bit (the guards change no arithmetic).  Only valid inputs run
@@ -40,6 +41,6 @@ def _run(lib, out):
 def test_checked_build_records_nothing_and_matches(checked_lib, tmp_path):
     want = _run(_capi.LIB_PATH, tmp_path / "normal.npz")
     got = _run(checked_lib, tmp_path / "checked.npz")
-    assert sorted(got.files) == sorted(want.files) and len(want.files) == 3 * 2 * 5
+    assert sorted(got.files) == sorted(want.files) and len(want.files) == 3 * 3 * 5 + 1 + 3 * 3
     for k in want.files:
         assert np.array_equal(got[k], want[k]), k
