@@ -861,8 +861,9 @@ __device__ __forceinline__ void tma_pipeline(int ntiles, int* err, Coords coords
 // plays in the CTA's k-th tile (warp rotation, above).
 template <int NT = kFwdThreads>
 __device__ __forceinline__ int rotated_thread(int k) {
-    static_assert((NT & (NT - 1)) == 0, "the rotation wraps a power of two");
-    return (int)((threadIdx.x + ((unsigned)k << 5)) & (NT - 1));
+    static_assert(NT % 32 == 0, "whole warps");
+    if constexpr ((NT & (NT - 1)) == 0) return (int)((threadIdx.x + ((unsigned)k << 5)) & (NT - 1));
+    else return (int)((threadIdx.x + ((unsigned)k % (NT / 32)) * 32u) % (unsigned)NT);
 }
 
 template <int FP>
