@@ -1,7 +1,7 @@
 """The FWI loop on the config-5 workload (2000x600, nt 5000, order 8, 96 shots).
 
     python -m cuda_fwi_gb300.fwi_demo [--iters 2] [--shots 96] [--nt 5000] [--snapshots 32]
-                                      [--restart STEP]
+                                      [--restart STEP] [--resume FILE]
 
 Observed data come from the true model (faulted, folded 30-layer medium with
 a wedge and a salt body) by a batched forward on the GPU; the inversion starts
@@ -9,7 +9,9 @@ from the true model smoothed with sigma = 300 m and runs fwi_psv_fwi_run
 (summed shot gradients with energy preconditioning, parabolic step-length
 search with batched trial forwards, bounded update).  --restart STEP retries
 a search that finds no step lowering the misfit once from STEP (the reference
-would stop there; the loop then continues).  One line per
+would stop there; the loop then continues).  --resume FILE saves the loop
+state there after each iteration and continues from it when the file exists
+(a run cut short picks up where it stopped).  One line per
 iteration: misfit, step length, trials, model error against the true model,
 seconds; then a JSON summary.
 """
@@ -34,6 +36,7 @@ def main(argv=None):
     ap.add_argument("--snapshots", type=int, default=32)
     ap.add_argument("--restart", type=float, default=0.0,
                     help="retry a failed step search once from this step (0 = stop, as the reference)")
+    ap.add_argument("--resume", default=None, help="resume file of the FWI loop (saved after each iteration)")
     a = ap.parse_args(argv)
     true = P.config5(True, nshots=a.shots)
     start = P.config5(False, nshots=a.shots)
@@ -50,7 +53,8 @@ def main(argv=None):
         err0 = float(np.sqrt(np.mean([np.sum((m0 - m1) ** 2) / np.sum(m1 ** 2) for m0, m1 in
                                       zip((start.lam, start.mu, start.rho), (true.lam, true.mu, true.rho))])))
         (lam, mu, rho), log = e.fwi_run(shots, obs, a.iters, step_length=0.01, order="summed", trial="sum",
-                                        true_model=(true.lam, true.mu, true.rho), restart_step=a.restart)
+                                        true_model=(true.lam, true.mu, true.rho), restart_step=a.restart,
+                                        resume_file=a.resume)
     for i, r in enumerate(log):
         print(f"iteration {i + 1}: misfit {r['misfit']:.6e}  step {r['step_length']:.4e}  trials {r['trials']}  "
               f"status {r['status']}  model error {r['model_error']:.6f}  {r['seconds']:.1f} s", flush=True)
